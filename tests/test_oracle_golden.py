@@ -1,0 +1,93 @@
+"""The oracle restates the reference's blocking and schedule bit-exactly.
+
+Pinned against fixtures produced by the reference's own block.cu
+(tests/golden/make_golden.py): block ids, levels, nnz, stratum/group
+membership and order, coe weights and per-slot entry order.
+"""
+import numpy as np
+import pytest
+
+import goldens
+import oracle
+
+CASES = goldens.cases()
+
+
+@pytest.fixture(scope="module", params=CASES)
+def case(request):
+    c = goldens.Case(request.param)
+    s = oracle.Schedule(c.shuffled, *c.dims, c.meta["block_s"], c.meta["parallel_sequence_size"])
+    return c, s
+
+
+def test_blocks_match_reference(case):
+    c, s = case
+    assert c.header["num_block_total"] == s.nblocks
+    nonempty = [b for b in range(s.nblocks) if s.block_nnz[b] > 0]
+    assert len(nonempty) == len(c.blocks)
+    for b, rb in zip(nonempty, c.blocks):
+        assert rb["id"] == b
+        assert rb["nnz"] == int(s.block_nnz[b])
+        assert rb["levels"] == tuple(int(v) for v in s.block_levels[b])
+        assert rb["ids"] == tuple(s.id_string(b, a) for a in range(3))
+
+
+def test_strata_and_groups_match_reference(case):
+    c, s = case
+    assert c.header["conflict_free_sequence_count"] == s.nstrata
+    assert c.header["conflict_free_max_parallel_blocks"] == s.max_parallel_cf
+    assert c.header["target_gpu_blocks"] == s.target
+    assert [q["ids"] for q in c.seqs] == s.groups
+    assert c.schedule["num_parallel"] == s.ngroups + 1
+    assert c.schedule["max_parallel"] == s.max_parallel
+    assert c.schedule["num_bs"] == [len(g) for g in s.groups]
+
+
+def test_slots_match_reference(case):
+    c, s = case
+    slots = c.schedule["slots"]
+    assert len(slots) == s.nslots
+    for k, sl in enumerate(slots):
+        b = int(s.slot_ids[k])
+        assert sl["id"] == b
+        assert sl["coe"] == tuple(float(v) for v in s.slot_coe[k])  # bit-exact
+        mine = [tuple(int(v) for v in c.shuffled[e]) for e in s.block_entries[b]]
+        assert mine == sl["xyz"]
+
+
+def test_fixtures_cover_quirks():
+    """The fixture set exercises the reference quirks the builder must keep."""
+    seen = dict(dup=False, empty=False, q3=False, multi_pad=False)
+    for name in CASES:
+        c = goldens.Case(name)
+        s = oracle.Schedule(c.shuffled, *c.dims, c.meta["block_s"], c.meta["parallel_sequence_size"])
+        seen["dup"] |= s.counters["duplicating"] > 0
+        seen["empty"] |= s.counters["empty_resplit"] > 0
+        seen["multi_pad"] |= s.nslots > len(set(s.slot_ids.tolist()))
+        # Q3: entries outside their block's prefix range (split on the global-level bit)
+        for b in range(s.nblocks):
+            if s.block_nnz[b] == 0:
+                continue
+            L = int(s.block_levels[b, 0])
+            g = s.global_levels[0]
+            code = int(s.block_codes[b, 0])
+            for e in s.block_entries[b][:64]:
+                n2 = oracle.hx(c.dims[0], g, int(c.shuffled[e, 0]))
+                pre = (n2 >> (g - L)) & ((1 << (L - 1)) - 1) if L > 1 else 0
+                if pre != code:
+                    seen["q3"] = True
+                    break
+    assert all(seen.values()), seen
+
+
+def test_hx_float_rounding():
+    """hx divides in float: near the top of a 5M axis the bucket differs from
+    the exact integer quotient (block.cu:41-42)."""
+    I = 4999999
+    diffs = 0
+    for num in range(I - 4000, I):
+        for level in (20, 22, 23):
+            exact = (num * (1 << (level - 1))) // (I + 1)
+            if oracle.hx(I, level, num) != exact:
+                diffs += 1
+    assert diffs > 0
