@@ -1,0 +1,342 @@
+#!/usr/bin/env python3
+"""Throughput of one CP-SGD epoch on one GB300 (nnz-updates/s).
+
+Workload (default, "c2"): the skewed medium tensor -- I = J = 100,000,
+K = 10,000, 50M unique entries with every mode's index Zipf(1.2), values from
+a rank-16 ground-truth CP (factors N(0, 0.5)) plus N(0, 0.05) noise, 90/10
+train/test split, rank R = 32, lr 0.005, lambda 0.02, factors U(0, 0.1).
+Data are seeded synthetic stand-ins generated in memory; the schedule is the
+reference's blocking (block_s 2048, 8 blocks per stratum).
+
+A step is one epoch: every scheduled slot's entries updated once.
+  value      updates/s of the epoch kernels with everything resident in HBM,
+             timed with CUDA events on the launching stream (K epochs
+             back to back, warm-up W epochs first)
+  e2e        the same metric through the C ABI's host-buffer call
+             (btc_train_epoch_host): factors uploaded from pinned host
+             memory, one epoch, test metrics, factors read back
+  roofline   algorithmic bytes per update (12 index + 4 value + 6*R*4 row
+             bytes) x updates / kernel time, against the measured HBM copy
+             bandwidth
+  cpu_baseline  the reference update rule replayed serially (FP64) on one
+             host core over a bounded sample of the same schedule
+
+--impl reference times the reference's update rule replayed on all host
+cores (Hogwild threads, FP64) on a bounded sample of the same schedule.
+
+Multi-GPU: the path does not shard (a single tensor's schedule is serial
+between strata); --gpus N under torchrun runs N independent replicas
+(weak scaling), with a barrier and the max time over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "btc-gpu_gb300", "python"))
+
+WORKLOADS = {
+    "c2": dict(I=100000, J=100000, K=10000, nnz=50_000_000, zipf=(1.2, 1.2, 1.2), gt_rank=16,
+               noise=0.05, train=0.9, R=32, lr=0.005, reg=0.02,
+               desc="skewed medium: I=J=100k K=10k, 50M nnz Zipf(1.2) per mode, rank-16 GT + N(0,0.05), "
+                    "90/10 split, R=32, lr 0.005, lambda 0.02"),
+    "c1": dict(I=1000, J=1000, K=1000, nnz=1_000_000, zipf=(0.0, 0.0, 0.0), gt_rank=8, noise=0.01,
+               train=0.9, R=16, lr=0.01, reg=0.01,
+               desc="plain small: I=J=K=1000, 1M nnz uniform, rank-8 GT + N(0,0.01), 90/10 split, R=16, "
+                    "lr 0.01, lambda 0.01"),
+    "small": dict(I=20000, J=20000, K=5000, nnz=2_000_000, zipf=(1.2, 1.2, 1.2), gt_rank=16, noise=0.05,
+                  train=0.9, R=32, lr=0.005, reg=0.02,
+                  desc="small skewed: I=J=20k K=5k, 2M nnz Zipf(1.2), R=32"),
+}
+METRIC = "nnz-updates/s & time-to-test-RMSE, tuned vs plain FP32, 1×GB300, % HBM peak"
+SEED = 20261203 + 1
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [v.strip() for v in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_workload(name, rank0=True):
+    import btc_gpu as bg
+
+    w = WORKLOADS[name]
+    t0 = time.time()
+    tx, tv, sx, sv = bg.gen_tensor(w["I"], w["J"], w["K"], w["nnz"], zipf=w["zipf"], gt_rank=w["gt_rank"],
+                                   gt_std=0.5, noise_std=w["noise"], train_frac=w["train"], seed=SEED)
+    bg.shuffle(tx, tv)
+    t1 = time.time()
+    return w, tx, tv, sx, sv, t1 - t0
+
+
+def cfg_for(w, dtype, mode, device=0):
+    import btc_gpu as bg
+
+    return bg.config(I=w["I"], J=w["J"], K=w["K"], rank=w["R"], lr=w["lr"], reg=w["reg"], block_s=2048,
+                     parallel_sequence_size=8, dtype=dtype, mode=mode, device=device)
+
+
+def flat_schedule(sched):
+    import oracle
+
+    off, ids, coe = sched.groups()
+    return oracle.FlatSchedule(off, ids, coe, sched.block_entries)
+
+
+def init_factors(w):
+    rng = np.random.default_rng(SEED)
+    return [rng.uniform(0.0, 0.1, (n, w["R"])) for n in (w["I"], w["J"], w["K"])]
+
+
+def cpu_sample(flat, tx, tv, w, budget_s, threads):
+    """Replay groups of the schedule until about budget_s has elapsed."""
+    A, B, C = init_factors(w)
+    done_upd, done_t, g = 0, 0.0, 0
+    step = max(1, flat.ngroups // 200)
+    while g < flat.ngroups and done_t < budget_s:
+        g1 = min(flat.ngroups, g + step)
+        t = time.perf_counter()
+        if threads == 1:
+            s0, s1 = int(flat.goff[g]), int(flat.goff[g1])
+            u = flat.replay(tx, tv, w["R"], w["lr"], w["reg"], A, B, C, s0, s1)
+        else:
+            u = flat.replay_mt(tx, tv, w["R"], w["lr"], w["reg"], A, B, C, threads, g, g1)
+        done_t += time.perf_counter() - t
+        done_upd += u
+        g = g1
+    return done_upd, done_t, g
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import btc_gpu as bg
+
+    w, tx, tv, sx, sv, _ = build_workload(args.workload)
+    cfg = cfg_for(w, bg.F64, bg.HOGWILD)
+    cfg.resident_blocks = -1
+    sched = bg.Schedule(cfg, tx)
+    flat = flat_schedule(sched)
+    threads = os.cpu_count() or 1
+    per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup))
+    for _ in range(args.warmup):
+        cpu_sample(flat, tx, tv, w, per_step / 4, threads)
+    ups, times = [], []
+    for _ in range(args.steps):
+        u, t, g = cpu_sample(flat, tx, tv, w, per_step, threads)
+        ups.append(u)
+        times.append(t)
+    value = sum(ups) / sum(times)
+    sample = ("first %d of %d strata of one epoch per step (%.0f updates/step), FP64 Hogwild threads, "
+              "schedule identical to the reference's block_problem" % (g, flat.ngroups, np.mean(ups)))
+    line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "updates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * np.mean(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": w["desc"]},
+            "cpu_baseline": {"value": value, "unit": "updates/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import btc_gpu as bg
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist = dist_mod
+        dist.init_process_group("gloo")
+    dtype = {"f32": bg.F32, "f64": bg.F64, "bf16": bg.BF16}[args.dtype]
+    mode = {"hogwild": bg.HOGWILD, "deterministic": bg.DETERMINISTIC, "staged": bg.STAGED}[args.mode]
+
+    w, tx, tv, sx, sv, tgen = build_workload(args.workload)
+    cfg = cfg_for(w, dtype, mode, device=local)
+    t = time.time()
+    sched = bg.Schedule(cfg, tx)
+    tsched = time.time() - t
+    sm = sched.summary
+    log("workload %s: train %d test %d, gen %.1fs schedule %.1fs; blocks %d strata %d groups %d slots %d "
+        "updates/epoch %d" % (args.workload, len(tv), len(sv), tgen, tsched, sm.num_blocks, sm.num_strata,
+                              sm.num_groups, sm.num_slots, sm.scheduled_updates))
+    ctx = bg.Context(cfg, sched, tx, tv, sx, sv)
+    init = init_factors(w)
+    for m in range(3):
+        ctx.set_factors(m, init[m])
+    ctx.train_epochs(args.warmup)
+    rm0 = ctx.eval(bg.TEST).rmse
+
+    clocks = Clocks(local)
+    if dist:
+        dist.barrier()
+    clocks.start()
+    st = ctx.train_epochs(args.steps)
+    clk = clocks.stop()
+    ms = st.kernel_ms
+    if dist:
+        import torch
+
+        tt = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    upd_per_step = sm.scheduled_updates
+    value = upd_per_step * args.steps * world / (ms / 1000.0)
+    rm1 = ctx.eval(bg.TEST).rmse
+
+    # end to end through the host-buffer call
+    shapes = [(n, w["R"]) for n in (w["I"], w["J"], w["K"])]
+    pinned = [bg.PinnedArray(s) for s in shapes]
+    for p, a in zip(pinned, init):
+        p.array[...] = a
+    e2e_steps = max(1, min(args.steps, 5))
+    ctx.train_epoch_host(*(p.array for p in pinned))
+    if dist:
+        dist.barrier()
+    t = time.perf_counter()
+    for _ in range(e2e_steps):
+        _, met = ctx.train_epoch_host(*(p.array for p in pinned))
+    e2e_s = time.perf_counter() - t
+    if dist:
+        import torch
+
+        tt = torch.tensor([e2e_s], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    fac_bytes = sum(n * w["R"] * 8 for n in (w["I"], w["J"], w["K"]))
+    e2e = {"value": upd_per_step * e2e_steps * world / e2e_s, "unit": "updates/s",
+           "h2d_bytes_per_step": fac_bytes, "d2h_bytes_per_step": fac_bytes + 24}
+
+    peak, src = peaks()
+    s_f = {"f32": 4, "f64": 8, "bf16": 2}[args.dtype]
+    s_v = 8 if args.dtype == "f64" else 4
+    b_upd = 12 + s_v + 6 * w["R"] * s_f
+    per_launch_ms = ms / max(1, st.launches)
+    upd_per_launch = upd_per_step * args.steps / max(1, st.launches)
+    achieved = b_upd * upd_per_launch / (per_launch_ms / 1000.0) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "peak_source": src, "bytes_per_update": b_upd,
+                "kernel": "k_hogwild" if mode == bg.HOGWILD else "k_det"}
+
+    line = None
+    if rank == 0:
+        flat = flat_schedule(sched)
+        u, tcpu, g = cpu_sample(flat, tx, tv, w, args.cpu_seconds, 1)
+        cpu = {"value": u / tcpu, "unit": "updates/s", "cores": 1, "kind": "port",
+               "sample": "first %d of %d strata of one epoch (%d updates), serial FP64 replay of the "
+                         "reference update rule" % (g, flat.ngroups, u)}
+        line = {"metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
+                "config": {"workload": w["desc"], "precision": args.dtype, "mode": args.mode,
+                           "train_nnz": int(len(tv)), "updates_per_epoch": int(upd_per_step),
+                           "parallelism": "replicas" if world > 1 else "single",
+                           "l2": "inputs larger than L2: entry stream %.2f GB per epoch; factor rows "
+                                 "(%.0f MB) stay L2-resident as in a real run" %
+                                 (upd_per_step * 16 / 1e9, sum(n * w["R"] * s_f for n in
+                                                             (w["I"], w["J"], w["K"])) / 1e6)},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": st.launches,
+                "train_nnz_per_s": len(tv) * args.steps * world / (ms / 1000.0),
+                "test_rmse": {"after_warmup": rm0, "after_timed": rm1, "e2e_last": met.rmse}}
+        if clk:
+            line["clocks"] = clk
+        print(json.dumps(line), flush=True)
+    for p in pinned:
+        p.free()
+    ctx.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--dtype", default="f32", choices=["f32", "f64", "bf16"])
+    ap.add_argument("--mode", default="hogwild", choices=["hogwild", "deterministic", "staged"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,725 @@
+// C ABI of the GB300 CP-SGD path (include/btc_gpu.h): configuration, host
+// schedule and the device context that replaces sgd_train's state.
+//
+// Device layout of one context (all in HBM, one allocation per array):
+//   coo        int4 per scheduled entry: (x, y, z, float value bits), blocks
+//              stored once, contiguously, in order of first use by the
+//              schedule, so one epoch streams the array front to back
+//   val64      FP64 value per entry (f64 contexts only)
+//   slot_off / slot_nnz / slot_coe   per scheduled slot (a block may occupy
+//              several slots: the reference pads strata with blocks already
+//              scheduled elsewhere, block.cu:686-690)
+//   items      (slot, first entry) work items of `chunk` entries, schedule order
+//   A, B, C    factor rows, row stride Rp (rank rounded up to the kernel's
+//              vector width, padding kept at zero)
+//   eval_*     train and test entries for the metrics kernel
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <limits>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "btc_gpu.h"
+#include "common.h"
+#include "kernels.h"
+#include "schedule.h"
+
+struct btc_schedule {
+    btc::Schedule s;
+};
+
+struct btc_ctx {
+    btc_config cfg{};
+    int dtype = 0, mode = 0, R = 0, Rp = 0, esize = 4;
+    int sms = 0, hw_grid = 0, hw_block = 256, chunk = 128, metric_grid = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int4* coo = nullptr;
+    double* val64 = nullptr;
+    long long* slot_off = nullptr;
+    int* slot_nnz = nullptr;
+    void* slot_coe = nullptr;
+    int2* items = nullptr;
+    long long nitems = 0;
+    void* F[3] = {nullptr, nullptr, nullptr};
+    int64_t rows[3] = {0, 0, 0};
+    int4* eval_coo[2] = {nullptr, nullptr};
+    double* eval_val[2] = {nullptr, nullptr};
+    int64_t eval_n[2] = {0, 0};
+    double* partials = nullptr;
+    double* result = nullptr;
+    double* staging = nullptr;  // double [max rows][R] for factor transfers
+    int* wave_slots = nullptr;
+    std::vector<int> wave_off;
+    int64_t updates = 0;
+    int nslots = 0;
+    bool failed = false;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+btc_status cuda_fail(cudaError_t e, const char* what)
+{
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return BTC_ERR_CUDA;
+}
+
+#define CK(call)                                  \
+    do {                                          \
+        cudaError_t e_ = (call);                  \
+        if (e_ != cudaSuccess)                    \
+            return cuda_fail(e_, #call);          \
+    } while (0)
+
+int default_threads(const btc_config& c)
+{
+    return c.host_threads > 0 ? c.host_threads : (int)std::max(1u, std::thread::hardware_concurrency());
+}
+
+int resident_blocks(const btc_config& c)
+{
+    if (c.resident_blocks != 0)
+        return c.resident_blocks < 0 ? 0 : c.resident_blocks;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        return 0;
+    }
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, c.device < n ? c.device : 0) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int per = p.maxBlocksPerMultiProcessor > 0 ? p.maxBlocksPerMultiProcessor : 32;
+    return p.multiProcessorCount * per;
+}
+
+template <typename T>
+void free_dev(T*& p)
+{
+    if (p)
+        cudaFree((void*)p);
+    p = nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* btc_status_string(btc_status s)
+{
+    switch (s) {
+    case BTC_OK: return "ok";
+    case BTC_ERR_ARG: return "invalid argument";
+    case BTC_ERR_CUDA: return g_last_error.empty() ? "CUDA error" : g_last_error.c_str();
+    case BTC_ERR_ALLOC: return "allocation failed";
+    case BTC_ERR_STATE: return "invalid state";
+    case BTC_ERR_IO: return "I/O error";
+    case BTC_ERR_TIMEOUT: return "device wait timed out";
+    case BTC_ERR_UNSUPPORTED: return "unsupported";
+    case BTC_ERR_RANGE: return "value out of range";
+    case BTC_ERR_NO_DEVICE: return "no CUDA device";
+    case BTC_ERR_DEVICE: return "kernel reported an error";
+    }
+    return "unknown status";
+}
+
+int32_t btc_abi_version(void) { return BTC_ABI_VERSION; }
+
+btc_status btc_config_default(btc_config* c)
+{
+    if (!c)
+        return BTC_ERR_ARG;
+    std::memset(c, 0, sizeof(*c));
+    c->I = 144;
+    c->J = 288;
+    c->K = 168;
+    c->epochs = 1000;
+    c->rank = 16;
+    c->lr = 0.005;
+    c->reg = 0.0005;
+    c->block_s = 2048;
+    c->thread_size = 512;
+    c->parallel_sequence_size = 8;
+    c->requested_gpu_count = 4;
+    c->dtype = BTC_DTYPE_F32;
+    c->mode = BTC_MODE_HOGWILD;
+    return BTC_OK;
+}
+
+btc_status btc_config_validate(const btc_config* c)
+{
+    if (!c)
+        return BTC_ERR_ARG;
+    if (c->I <= 0 || c->J <= 0 || c->K <= 0 || c->epochs <= 0)
+        return BTC_ERR_ARG;
+    if (c->rank <= 0 || c->rank > btc::kMaxRank)
+        return BTC_ERR_ARG;
+    if (!(c->lr > 0) || !(c->reg >= 0) || c->block_s <= 0)
+        return BTC_ERR_ARG;
+    if (c->thread_size <= 0 || c->thread_size > 1024 || c->parallel_sequence_size < 0 ||
+        c->requested_gpu_count < 0)
+        return BTC_ERR_ARG;
+    if (c->dtype < 0 || c->dtype > 2 || c->mode < 0 || c->mode > 2 || c->chunk < 0)
+        return BTC_ERR_ARG;
+    return BTC_OK;
+}
+
+/* ---- schedule ---- */
+
+btc_status btc_schedule_build(const btc_config* cfg, const int32_t* xyz, int64_t n, btc_schedule** out)
+{
+    if (!cfg || !out || (n > 0 && !xyz))
+        return BTC_ERR_ARG;
+    *out = nullptr;
+    btc_schedule* s = new (std::nothrow) btc_schedule();
+    if (!s)
+        return BTC_ERR_ALLOC;
+    btc_status rc;
+    try {
+        rc = btc::build_schedule(*cfg, xyz, n, resident_blocks(*cfg), default_threads(*cfg), s->s);
+    } catch (const std::bad_alloc&) {
+        rc = BTC_ERR_ALLOC;
+    }
+    if (rc != BTC_OK) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return BTC_OK;
+}
+
+btc_status btc_schedule_summarize(const btc_schedule* sp, btc_schedule_summary* o)
+{
+    if (!sp || !o)
+        return BTC_ERR_ARG;
+    const btc::Schedule& s = sp->s;
+    std::memset(o, 0, sizeof(*o));
+    o->num_blocks = (int32_t)s.blocks.size();
+    for (const auto& b : s.blocks)
+        o->nonempty_blocks += b.ent.empty() ? 0 : 1;
+    o->num_strata = (int32_t)s.strata_off.size() - 1;
+    o->max_parallel_cf = s.max_parallel_cf;
+    o->target_gpu_blocks = s.target;
+    o->num_groups = (int32_t)s.group_off.size() - 1;
+    o->num_slots = (int32_t)s.slot_block.size();
+    o->max_parallel = s.max_parallel;
+    o->scheduled_updates = s.scheduled_updates;
+    o->train_nnz = s.train_nnz;
+    for (int a = 0; a < 3; a++) {
+        o->global_levels[a] = s.global_levels[a];
+        o->build_seconds[a] = s.seconds[a];
+    }
+    return BTC_OK;
+}
+
+btc_status btc_schedule_blocks(const btc_schedule* sp, int32_t* meta, uint64_t* codes)
+{
+    if (!sp || !meta || !codes)
+        return BTC_ERR_ARG;
+    const auto& B = sp->s.blocks;
+    for (size_t i = 0; i < B.size(); i++) {
+        meta[4 * i] = (int32_t)B[i].ent.size();
+        for (int a = 0; a < 3; a++) {
+            meta[4 * i + 1 + a] = B[i].level[a];
+            codes[3 * i + a] = B[i].code[a];
+        }
+    }
+    return BTC_OK;
+}
+
+btc_status btc_schedule_block_entries(const btc_schedule* sp, int32_t b, int32_t* out, int32_t* n)
+{
+    if (!sp || !n || b < 0 || b >= (int32_t)sp->s.blocks.size())
+        return BTC_ERR_ARG;
+    const auto& e = sp->s.blocks[b].ent;
+    if (*n < (int32_t)e.size() || (!out && !e.empty())) {
+        *n = (int32_t)e.size();
+        return BTC_ERR_ARG;
+    }
+    if (!e.empty())
+        std::memcpy(out, e.data(), e.size() * sizeof(int32_t));
+    *n = (int32_t)e.size();
+    return BTC_OK;
+}
+
+btc_status btc_schedule_strata(const btc_schedule* sp, int32_t* off, int32_t* ids)
+{
+    if (!sp || !off || !ids)
+        return BTC_ERR_ARG;
+    std::copy(sp->s.strata_off.begin(), sp->s.strata_off.end(), off);
+    std::copy(sp->s.strata_ids.begin(), sp->s.strata_ids.end(), ids);
+    return BTC_OK;
+}
+
+btc_status btc_schedule_groups(const btc_schedule* sp, int32_t* off, int32_t* slot_block, double* coe)
+{
+    if (!sp || !off || !slot_block || !coe)
+        return BTC_ERR_ARG;
+    std::copy(sp->s.group_off.begin(), sp->s.group_off.end(), off);
+    std::copy(sp->s.slot_block.begin(), sp->s.slot_block.end(), slot_block);
+    std::copy(sp->s.slot_coe.begin(), sp->s.slot_coe.end(), coe);
+    return BTC_OK;
+}
+
+btc_status btc_schedule_write_report(const btc_schedule* sp, const btc_config*, const char* path)
+{
+    if (!sp || !path)
+        return BTC_ERR_ARG;
+    std::ofstream f(path, std::ios::out | std::ios::trunc | std::ios::binary);
+    if (!f.is_open())
+        return BTC_ERR_IO;
+    f << btc::report_text(sp->s);
+    return f.good() ? BTC_OK : BTC_ERR_IO;
+}
+
+void btc_schedule_free(btc_schedule* s) { delete s; }
+
+/* ---- device context ---- */
+
+btc_status btc_ctx_destroy(btc_ctx* c)
+{
+    if (!c)
+        return BTC_OK;
+    int dev = c->cfg.device;
+    cudaSetDevice(dev);
+    if (c->stream)
+        cudaStreamSynchronize(c->stream);
+    free_dev(c->coo);
+    free_dev(c->val64);
+    free_dev(c->slot_off);
+    free_dev(c->slot_nnz);
+    free_dev(c->slot_coe);
+    free_dev(c->items);
+    for (int a = 0; a < 3; a++)
+        free_dev(c->F[a]);
+    for (int k = 0; k < 2; k++) {
+        free_dev(c->eval_coo[k]);
+        free_dev(c->eval_val[k]);
+    }
+    free_dev(c->partials);
+    free_dev(c->result);
+    free_dev(c->staging);
+    free_dev(c->wave_slots);
+    if (c->ev0)
+        cudaEventDestroy(c->ev0);
+    if (c->ev1)
+        cudaEventDestroy(c->ev1);
+    if (c->stream)
+        cudaStreamDestroy(c->stream);
+    delete c;
+    return BTC_OK;
+}
+
+static btc_status upload(void** dst, const void* src, size_t bytes, cudaStream_t st)
+{
+    CK(cudaMalloc(dst, bytes > 0 ? bytes : 16));
+    if (bytes > 0)
+        CK(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, st));
+    return BTC_OK;
+}
+
+static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* txyz, const double* tval,
+                            int64_t ntr, const int32_t* sxyz, const double* sval, int64_t nte)
+{
+    const btc_config& cfg = c->cfg;
+    CK(cudaSetDevice(cfg.device));
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, cfg.device));
+    c->sms = prop.multiProcessorCount;
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&c->ev0));
+    CK(cudaEventCreate(&c->ev1));
+    c->dtype = cfg.dtype;
+    c->mode = cfg.mode;
+    if (c->dtype == BTC_DTYPE_BF16 || c->mode == BTC_MODE_STAGED)
+        return BTC_ERR_UNSUPPORTED;
+    c->esize = c->dtype == BTC_DTYPE_F64 ? 8 : 4;
+    c->R = cfg.rank;
+    c->Rp = btc::padded_rank(c->dtype, c->R);
+    c->chunk = cfg.chunk > 0 ? cfg.chunk : 128;
+    c->rows[0] = cfg.I;
+    c->rows[1] = cfg.J;
+    c->rows[2] = cfg.K;
+
+    // entry stream: each scheduled block once, in order of first use
+    const int nslots = (int)s.slot_block.size();
+    c->nslots = nslots;
+    std::vector<long long> boff(s.blocks.size(), -1);
+    long long total = 0;
+    for (int k = 0; k < nslots; k++) {
+        int b = s.slot_block[k];
+        if (boff[b] < 0) {
+            boff[b] = total;
+            total += (long long)s.blocks[b].ent.size();
+        }
+    }
+    std::vector<int4> coo((size_t)total);
+    std::vector<double> v64(c->dtype == BTC_DTYPE_F64 ? (size_t)total : 0);
+    for (size_t b = 0; b < s.blocks.size(); b++) {
+        if (boff[b] < 0)
+            continue;
+        long long o = boff[b];
+        for (int32_t e : s.blocks[b].ent) {
+            float fv = (float)tval[e];
+            int4 q;
+            q.x = txyz[3 * (int64_t)e];
+            q.y = txyz[3 * (int64_t)e + 1];
+            q.z = txyz[3 * (int64_t)e + 2];
+            std::memcpy(&q.w, &fv, 4);
+            coo[(size_t)o] = q;
+            if (!v64.empty())
+                v64[(size_t)o] = tval[e];
+            o++;
+        }
+    }
+    std::vector<long long> soff(nslots);
+    std::vector<int> snnz(nslots);
+    std::vector<double> coe64(3 * (size_t)nslots);
+    std::vector<float> coe32(3 * (size_t)nslots);
+    std::vector<int2> items;
+    c->updates = 0;
+    for (int k = 0; k < nslots; k++) {
+        int b = s.slot_block[k];
+        soff[k] = boff[b];
+        snnz[k] = (int)s.blocks[b].ent.size();
+        c->updates += snnz[k];
+        for (int a = 0; a < 3; a++) {
+            coe64[3 * k + a] = s.slot_coe[3 * k + a] * cfg.lr;  // (coe*lr) as the reference groups it
+            coe32[3 * k + a] = (float)coe64[3 * k + a];
+        }
+        for (int st = 0; st < snnz[k]; st += c->chunk)
+            items.push_back(make_int2(k, st));
+    }
+    c->nitems = (long long)items.size();
+    btc_status rc;
+    if ((rc = upload((void**)&c->coo, coo.data(), coo.size() * sizeof(int4), c->stream)))
+        return rc;
+    if (!v64.empty() && (rc = upload((void**)&c->val64, v64.data(), v64.size() * 8, c->stream)))
+        return rc;
+    if ((rc = upload((void**)&c->slot_off, soff.data(), soff.size() * 8, c->stream)))
+        return rc;
+    if ((rc = upload((void**)&c->slot_nnz, snnz.data(), snnz.size() * 4, c->stream)))
+        return rc;
+    if (c->dtype == BTC_DTYPE_F64)
+        rc = upload(&c->slot_coe, coe64.data(), coe64.size() * 8, c->stream);
+    else
+        rc = upload(&c->slot_coe, coe32.data(), coe32.size() * 4, c->stream);
+    if (rc)
+        return rc;
+    if ((rc = upload((void**)&c->items, items.data(), items.size() * sizeof(int2), c->stream)))
+        return rc;
+
+    // evaluation entries
+    const int32_t* exyz[2] = {txyz, sxyz};
+    const double* eval[2] = {tval, sval};
+    int64_t en[2] = {ntr, nte};
+    for (int k = 0; k < 2; k++) {
+        std::vector<int4> q((size_t)en[k]);
+        for (int64_t i = 0; i < en[k]; i++)
+            q[(size_t)i] = make_int4(exyz[k][3 * i], exyz[k][3 * i + 1], exyz[k][3 * i + 2], 0);
+        if ((rc = upload((void**)&c->eval_coo[k], q.data(), q.size() * sizeof(int4), c->stream)))
+            return rc;
+        if ((rc = upload((void**)&c->eval_val[k], eval[k], (size_t)en[k] * 8, c->stream)))
+            return rc;
+        c->eval_n[k] = en[k];
+    }
+    c->metric_grid = c->sms * 4;
+    CK(cudaMalloc((void**)&c->partials, (size_t)c->metric_grid * 3 * sizeof(double)));
+    CK(cudaMalloc((void**)&c->result, 4 * sizeof(double)));
+
+    int64_t maxrows = std::max(c->rows[0], std::max(c->rows[1], c->rows[2]));
+    for (int a = 0; a < 3; a++) {
+        size_t bytes = (size_t)c->rows[a] * c->Rp * c->esize;
+        CK(cudaMalloc(&c->F[a], bytes));
+        CK(cudaMemsetAsync(c->F[a], 0, bytes, c->stream));
+    }
+    CK(cudaMalloc((void**)&c->staging, (size_t)maxrows * c->R * sizeof(double)));
+
+    int occ = btc::hogwild_blocks_per_sm(c->dtype, c->R, c->hw_block);
+    c->hw_grid = c->sms * std::max(1, occ);
+
+    if (c->mode == BTC_MODE_DETERMINISTIC) {
+        // slots that share any factor row run in schedule order; the others
+        // run together (wave = 1 + latest wave of any row the slot touches)
+        std::vector<int> last[3];
+        for (int a = 0; a < 3; a++)
+            last[a].assign((size_t)c->rows[a], 0);
+        std::vector<int> wave(nslots);
+        int nw = 0;
+        for (int k = 0; k < nslots; k++) {
+            const auto& ent = s.blocks[s.slot_block[k]].ent;
+            int w = 0;
+            for (int32_t e : ent)
+                for (int a = 0; a < 3; a++)
+                    w = std::max(w, last[a][(size_t)txyz[3 * (int64_t)e + a]]);
+            w += 1;
+            for (int32_t e : ent)
+                for (int a = 0; a < 3; a++)
+                    last[a][(size_t)txyz[3 * (int64_t)e + a]] = w;
+            wave[k] = w;
+            nw = std::max(nw, w);
+        }
+        c->wave_off.assign((size_t)nw + 2, 0);
+        for (int k = 0; k < nslots; k++)
+            c->wave_off[(size_t)wave[k] + 1]++;
+        for (int w = 1; w <= nw + 1; w++)
+            c->wave_off[(size_t)w] += c->wave_off[(size_t)w - 1];
+        std::vector<int> ws(nslots);
+        std::vector<int> fill(c->wave_off.begin(), c->wave_off.end());
+        for (int k = 0; k < nslots; k++)
+            ws[(size_t)fill[(size_t)wave[k]]++] = k;
+        if ((rc = upload((void**)&c->wave_slots, ws.data(), ws.size() * 4, c->stream)))
+            return rc;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return BTC_OK;
+}
+
+btc_status btc_ctx_create(const btc_config* cfg, const btc_schedule* s, const int32_t* txyz,
+                          const double* tval, int64_t ntr, const int32_t* sxyz, const double* sval,
+                          int64_t nte, btc_ctx** out)
+{
+    if (!cfg || !s || !out || (ntr > 0 && (!txyz || !tval)) || (nte > 0 && (!sxyz || !sval)))
+        return BTC_ERR_ARG;
+    *out = nullptr;
+    btc_status rc = btc_config_validate(cfg);
+    if (rc)
+        return rc;
+    if (s->s.train_nnz != ntr || s->s.I != cfg->I || s->s.J != cfg->J || s->s.K != cfg->K)
+        return BTC_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+        cudaGetLastError();
+        return BTC_ERR_NO_DEVICE;
+    }
+    if (cfg->device < 0 || cfg->device >= ndev)
+        return BTC_ERR_ARG;
+    btc_ctx* c = new (std::nothrow) btc_ctx();
+    if (!c)
+        return BTC_ERR_ALLOC;
+    c->cfg = *cfg;
+    try {
+        rc = ctx_build(c, s->s, txyz, tval, ntr, sxyz, sval, nte);
+    } catch (const std::bad_alloc&) {
+        rc = BTC_ERR_ALLOC;
+    }
+    if (rc) {
+        btc_ctx_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return BTC_OK;
+}
+
+void* btc_ctx_stream(btc_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+btc_status btc_ctx_set_factors(btc_ctx* c, int32_t mode, const double* host)
+{
+    if (!c || mode < 0 || mode > 2 || !host)
+        return BTC_ERR_ARG;
+    CK(cudaSetDevice(c->cfg.device));
+    size_t bytes = (size_t)c->rows[mode] * c->R * sizeof(double);
+    CK(cudaMemcpyAsync(c->staging, host, bytes, cudaMemcpyHostToDevice, c->stream));
+    CK(btc::launch_pack(c->dtype, c->staging, c->F[mode], c->rows[mode], c->R, c->Rp, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return BTC_OK;
+}
+
+btc_status btc_ctx_get_factors(btc_ctx* c, int32_t mode, double* host)
+{
+    if (!c || mode < 0 || mode > 2 || !host)
+        return BTC_ERR_ARG;
+    CK(cudaSetDevice(c->cfg.device));
+    size_t bytes = (size_t)c->rows[mode] * c->R * sizeof(double);
+    CK(btc::launch_unpack(c->dtype, c->F[mode], c->staging, c->rows[mode], c->R, c->Rp, c->stream));
+    CK(cudaMemcpyAsync(host, c->staging, bytes, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return BTC_OK;
+}
+
+btc_status btc_ctx_init_factors(btc_ctx* c, uint64_t seed, double lo, double hi)
+{
+    if (!c || !(hi >= lo))
+        return BTC_ERR_ARG;
+    for (int m = 0; m < 3; m++) {
+        std::vector<double> h((size_t)c->rows[m] * c->R);
+        for (int64_t r = 0; r < c->rows[m]; r++)
+            for (int q = 0; q < c->R; q++)
+                h[(size_t)r * c->R + q] = btc::init_uniform(seed, m, r, q, lo, hi);
+        btc_status rc = btc_ctx_set_factors(c, m, h.data());
+        if (rc)
+            return rc;
+    }
+    return BTC_OK;
+}
+
+static btc::SgdArgs sgd_args(btc_ctx* c)
+{
+    btc::SgdArgs a{};
+    a.coo = c->coo;
+    a.val64 = c->val64;
+    a.items = c->items;
+    a.nitems = c->nitems;
+    a.slot_off = c->slot_off;
+    a.slot_nnz = c->slot_nnz;
+    a.slot_coe = c->slot_coe;
+    a.A = c->F[0];
+    a.B = c->F[1];
+    a.C = c->F[2];
+    a.R = c->R;
+    a.Rp = c->Rp;
+    a.reg = c->cfg.reg;
+    a.chunk = c->chunk;
+    return a;
+}
+
+static btc_status enqueue_epoch(btc_ctx* c, int* launches)
+{
+    btc::SgdArgs a = sgd_args(c);
+    int n = 0;
+    if (c->mode == BTC_MODE_HOGWILD) {
+        CK(btc::launch_hogwild(c->dtype, a, c->hw_grid, c->hw_block, c->stream));
+        n = c->nitems > 0 ? 1 : 0;
+    } else if (c->mode == BTC_MODE_DETERMINISTIC) {
+        for (size_t w = 1; w + 1 < c->wave_off.size(); w++) {
+            int b = c->wave_off[w], e = c->wave_off[w + 1];
+            CK(btc::launch_det_wave(c->dtype, c->wave_slots + b, e - b, a, c->stream));
+            n += e > b ? 1 : 0;
+        }
+    } else {
+        return BTC_ERR_UNSUPPORTED;
+    }
+    if (launches)
+        *launches = n;
+    return BTC_OK;
+}
+
+btc_status btc_train_epoch(btc_ctx* c, btc_epoch_stats* st)
+{
+    if (!c)
+        return BTC_ERR_ARG;
+    CK(cudaSetDevice(c->cfg.device));
+    int launches = 0;
+    CK(cudaEventRecord(c->ev0, c->stream));
+    btc_status rc = enqueue_epoch(c, &launches);
+    if (rc)
+        return rc;
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(cudaEventSynchronize(c->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    if (st) {
+        st->kernel_ms = ms;
+        st->updates = c->updates;
+        st->launches = launches;
+        st->device_status = 0;
+    }
+    return BTC_OK;
+}
+
+btc_status btc_train_epochs(btc_ctx* c, int32_t n, btc_epoch_stats* st)
+{
+    if (!c || n < 0)
+        return BTC_ERR_ARG;
+    CK(cudaSetDevice(c->cfg.device));
+    int launches = 0, total = 0;
+    CK(cudaEventRecord(c->ev0, c->stream));
+    for (int32_t i = 0; i < n; i++) {
+        btc_status rc = enqueue_epoch(c, &launches);
+        if (rc)
+            return rc;
+        total += launches;
+    }
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(cudaEventSynchronize(c->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    if (st) {
+        st->kernel_ms = ms;
+        st->updates = c->updates * (int64_t)n;
+        st->launches = total;
+        st->device_status = 0;
+    }
+    return BTC_OK;
+}
+
+btc_status btc_host_alloc(void** p, int64_t bytes)
+{
+    if (!p || bytes < 0)
+        return BTC_ERR_ARG;
+    *p = nullptr;
+    CK(cudaHostAlloc(p, (size_t)std::max<int64_t>(bytes, 1), cudaHostAllocDefault));
+    return BTC_OK;
+}
+
+void btc_host_free(void* p)
+{
+    if (p)
+        cudaFreeHost(p);
+}
+
+static void finish_metrics(const double* r, int64_t n, btc_metrics* o)
+{
+    const double nan = std::numeric_limits<double>::quiet_NaN();
+    o->count = n;
+    o->sse = r[0];
+    o->sae = r[1];
+    o->ref2 = r[2];
+    if (n == 0) {
+        o->rmse = o->mae = o->er = nan;
+        return;
+    }
+    o->rmse = std::sqrt(r[0] / (double)n);
+    o->mae = r[1] / (double)n;
+    o->er = r[2] > 0 ? r[0] / r[2] : nan;
+}
+
+btc_status btc_eval(btc_ctx* c, int32_t split, btc_metrics* out)
+{
+    if (!c || !out || split < 0 || split > 1)
+        return BTC_ERR_ARG;
+    CK(cudaSetDevice(c->cfg.device));
+    double r[3] = {0, 0, 0};
+    int64_t n = c->eval_n[split];
+    if (n > 0) {
+        CK(btc::launch_metrics(c->dtype, c->eval_coo[split], c->eval_val[split], n, c->F[0], c->F[1],
+                               c->F[2], c->R, c->Rp, c->partials, c->metric_grid, c->result, c->stream));
+        CK(cudaMemcpyAsync(r, c->result, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    finish_metrics(r, n, out);
+    return BTC_OK;
+}
+
+btc_status btc_train_epoch_host(btc_ctx* c, double* A, double* B, double* C, btc_epoch_stats* st,
+                                btc_metrics* test)
+{
+    if (!c || !A || !B || !C)
+        return BTC_ERR_ARG;
+    double* H[3] = {A, B, C};
+    btc_status rc;
+    for (int m = 0; m < 3; m++)
+        if ((rc = btc_ctx_set_factors(c, m, H[m])))
+            return rc;
+    if ((rc = btc_train_epoch(c, st)))
+        return rc;
+    if (test && (rc = btc_eval(c, BTC_SPLIT_TEST, test)))
+        return rc;
+    for (int m = 0; m < 3; m++)
+        if ((rc = btc_ctx_get_factors(c, m, H[m])))
+            return rc;
+    return BTC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,604 @@
+// Host-side schedule builder (see schedule.h).
+//
+// Same results as the reference, different machinery:
+//  * blocking (block.cu:154-401): the tree keeps integer prefix codes instead
+//    of vector<bool> copies; each entry is routed by three float bucket codes
+//    computed exactly as hx does (block.cu:38-50), including the split bit
+//    taken at the GLOBAL level of the axis (block.cu:215-216, 285-286,
+//    353-354) and the re-split of a full or empty child (block.cu:237-253);
+//  * strata (block.cu:1024-1148): the reference's repeated greedy scans equal
+//    a first-fit assignment of blocks in ascending id order (a block joins the
+//    first stratum whose members it conflicts with on no axis), computed here
+//    with 64-bin interval masks as a prefilter;
+//  * padding (block.cu:545-565, 660-697): per group, candidates are scanned
+//    in (nnz, id) order so the first zero-conflict candidate ends the scan;
+//    groups are independent, so they are padded on several threads;
+//  * coe weights (block.cu:470-513): union-find per axis inside each group.
+#include "schedule.h"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <set>
+#include <sstream>
+#include <thread>
+
+namespace btc {
+namespace {
+
+double now_s()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct Node {
+    int32_t left = -1, right = -1, block = 0, h = 1;
+    int32_t len[3] = {1, 1, 1};
+    uint64_t code[3] = {0, 0, 0};
+};
+
+inline int axis_of_h(int h)
+{
+    int t = h % 3;
+    return t == 1 ? 0 : (t == 2 ? 1 : 2);
+}
+
+// hx (block.cu:38-50): n_1 = (end+1)/2^(level-1) rounded to float, then
+// floor(num / n_1) in float.
+struct Axis {
+    float n1[66];
+    void init(int end)
+    {
+        for (int l = 1; l <= 65; l++)
+            n1[l] = (float)((double)(end + 1) / std::ldexp(1.0, l - 1));
+    }
+    inline bool hx(int level, int num, int64_t& out) const
+    {
+        float q = (float)num / n1[level];
+        float f = std::floor(q);
+        if (!(f >= 0.0f) || f >= 2147483648.0f)
+            return false;
+        out = (int64_t)f;
+        return true;
+    }
+};
+
+inline uint64_t prefix_bits(int64_t n2, int g, int L)
+{
+    if (L <= 1)
+        return 0;
+    return ((uint64_t)n2 >> (g - L)) & ((1ULL << (L - 1)) - 1ULL);
+}
+
+inline uint64_t left_align(uint64_t code, int level)
+{
+    int m = level - 1;
+    return m == 0 ? 0 : code << (64 - m);
+}
+
+inline uint64_t bin_mask(uint64_t lcode, int level)
+{
+    int m = level - 1;
+    uint64_t first = lcode >> 58;
+    if (m >= 6)
+        return 1ULL << first;
+    int count = 1 << (6 - m);
+    uint64_t span = count == 64 ? ~0ULL : ((1ULL << count) - 1ULL);
+    return span << first;
+}
+
+// find_conflict_x (block.cu:413-430) on left-aligned codes
+inline bool axis_conflict(const BlockRec& a, const BlockRec& b, int ax)
+{
+    int m = std::min(a.level[ax], b.level[ax]) - 1;
+    if (m == 0)
+        return true;
+    return ((a.lcode[ax] ^ b.lcode[ax]) >> (64 - m)) == 0;
+}
+
+void finish_block_codes(BlockRec& b)
+{
+    for (int a = 0; a < 3; a++) {
+        b.lcode[a] = left_align(b.code[a], b.level[a]);
+        b.bins[a] = bin_mask(b.lcode[a], b.level[a]);
+    }
+}
+
+btc_status blocking(const int32_t* xyz, int64_t n, int I, int J, int K, int bs, Schedule& s)
+{
+    Axis ax[3];
+    ax[0].init(I);
+    ax[1].init(J);
+    ax[2].init(K);
+    int g[3] = {1, 1, 1};
+    std::vector<Node> nodes(1);
+    std::vector<BlockRec>& blocks = s.blocks;
+    blocks.clear();
+    blocks.reserve((size_t)std::max<int64_t>(16, n / std::max(1, bs) * 2));
+    blocks.emplace_back();
+    for (int a = 0; a < 3; a++) {
+        blocks[0].level[a] = 1;
+        blocks[0].code[a] = 0;
+    }
+    blocks[0].ent.reserve(bs);
+    std::vector<int32_t> t1, t2;
+    t1.reserve(bs + 1);
+    t2.reserve(bs + 1);
+
+    for (int64_t i = 0; i < n; i++) {
+        const int32_t* p = xyz + 3 * i;
+        int64_t pc[3];
+        for (int a = 0; a < 3; a++)
+            if (!ax[a].hx(g[a], p[a], pc[a]))
+                return BTC_ERR_RANGE;
+        int node = 0;
+        while (nodes[node].left >= 0) {
+            int a = axis_of_h(nodes[node].h);
+            const Node& lc = nodes[nodes[node].left];
+            node = prefix_bits(pc[a], g[a], lc.len[a]) == lc.code[a] ? nodes[node].left
+                                                                    : nodes[node].right;
+        }
+        int id = nodes[node].block;
+        if ((int)blocks[id].ent.size() < bs) {
+            blocks[id].ent.push_back((int32_t)i);
+            continue;
+        }
+        bool done = false;
+        while (!done) {
+            int a;
+            {
+                const BlockRec& B = blocks[id];
+                if (B.level[0] == B.level[1] && B.level[1] == B.level[2])
+                    a = 0;
+                else if (B.level[1] < B.level[0])
+                    a = 1;
+                else if (B.level[2] < B.level[1])
+                    a = 2;
+                else
+                    return BTC_ERR_STATE;
+            }
+            blocks[id].level[a]++;
+            if (blocks[id].level[a] > g[a])
+                g[a] = blocks[id].level[a];
+            if (g[a] > 63)
+                return BTC_ERR_RANGE;
+            // Create_Btree (block.cu:90-152)
+            int nb = (int)blocks.size();
+            {
+                int l = (int)nodes.size();
+                nodes.resize(nodes.size() + 2);
+                Node& P = nodes[node];
+                int ta = axis_of_h(P.h);
+                Node L = P, R = P;
+                L.h = R.h = P.h + 1;
+                L.left = L.right = R.left = R.right = -1;
+                L.len[ta] = R.len[ta] = P.len[ta] + 1;
+                L.code[ta] = P.code[ta] << 1;
+                R.code[ta] = (P.code[ta] << 1) | 1ULL;
+                L.block = id;
+                R.block = nb;
+                P.block = -1;
+                P.left = l;
+                P.right = l + 1;
+                nodes[l] = L;
+                nodes[l + 1] = R;
+            }
+            blocks.emplace_back();
+            BlockRec& NB = blocks[nb];
+            BlockRec& B = blocks[id];
+            for (int q = 0; q < 3; q++) {
+                NB.level[q] = B.level[q];
+                NB.code[q] = B.code[q];
+            }
+            NB.code[a] = (B.code[a] << 1) | 1ULL;
+            B.code[a] = B.code[a] << 1;
+            t1.clear();
+            t2.clear();
+            for (int32_t e : B.ent) {
+                int64_t hv;
+                if (!ax[a].hx(g[a], xyz[3 * (int64_t)e + a], hv))
+                    return BTC_ERR_RANGE;
+                ((hv & 1) == 0 ? t1 : t2).push_back(e);
+            }
+            int64_t hp;
+            if (!ax[a].hx(g[a], p[a], hp))
+                return BTC_ERR_RANGE;
+            int bit = (int)(hp & 1);
+            if ((int)t1.size() < bs && (int)t2.size() < bs) {
+                done = true;
+                (bit == 0 ? t1 : t2).push_back((int32_t)i);
+                B.ent.assign(t1.begin(), t1.end());
+                NB.ent.assign(t2.begin(), t2.end());
+            } else if (bit == 0) {
+                B.ent.assign(t1.begin(), t1.end());
+                NB.ent.assign(t2.begin(), t2.end());
+                node = nodes[node].left;
+            } else {
+                // the reference stores t1 then t2 into the NEW block; the old
+                // block keeps its previous entries (block.cu:244-253)
+                NB.ent.assign(t2.begin(), t2.end());
+                id = nb;
+                node = nodes[node].right;
+            }
+            if ((int)NB.ent.capacity() < bs)
+                NB.ent.reserve(bs);
+        }
+    }
+    for (auto& b : blocks)
+        finish_block_codes(b);
+    for (int a = 0; a < 3; a++)
+        s.global_levels[a] = g[a];
+    return BTC_OK;
+}
+
+// search_parallel_block_Tree as first-fit in ascending block id.
+void strata_first_fit(Schedule& s)
+{
+    struct St {
+        uint64_t bins[3] = {0, 0, 0};
+        std::vector<int32_t> mem;
+    };
+    std::vector<St> st;
+    const auto& B = s.blocks;
+    for (int32_t b = 0; b < (int32_t)B.size(); b++) {
+        if (B[b].ent.empty())
+            continue;
+        const BlockRec& cb = B[b];
+        size_t k = 0;
+        for (; k < st.size(); k++) {
+            St& S = st[k];
+            bool ok = true;
+            for (int a = 0; a < 3 && ok; a++) {
+                if ((S.bins[a] & cb.bins[a]) == 0)
+                    continue;
+                for (int32_t m : S.mem)
+                    if (axis_conflict(B[m], cb, a)) {
+                        ok = false;
+                        break;
+                    }
+            }
+            if (ok)
+                break;
+        }
+        if (k == st.size())
+            st.emplace_back();
+        St& S = st[k];
+        S.mem.push_back(b);
+        for (int a = 0; a < 3; a++)
+            S.bins[a] |= cb.bins[a];
+    }
+    s.strata_off.assign(1, 0);
+    s.strata_ids.clear();
+    s.max_parallel_cf = 0;
+    for (auto& S : st) {
+        s.strata_ids.insert(s.strata_ids.end(), S.mem.begin(), S.mem.end());
+        s.strata_off.push_back((int32_t)s.strata_ids.size());
+        s.max_parallel_cf = std::max<int32_t>(s.max_parallel_cf, (int32_t)S.mem.size());
+    }
+}
+
+// update_conflict_weights (block.cu:470-513) for one group
+void coe_weights(const std::vector<BlockRec>& B, const int32_t* ids, int n, double* coe)
+{
+    std::vector<int> par(n);
+    std::vector<long long> sum(n);
+    auto find = [&](int i) {
+        while (par[i] != i) {
+            par[i] = par[par[i]];
+            i = par[i];
+        }
+        return i;
+    };
+    for (int a = 0; a < 3; a++) {
+        for (int i = 0; i < n; i++) {
+            par[i] = i;
+            sum[i] = 0;
+        }
+        for (int i = 0; i < n; i++)
+            for (int j = i + 1; j < n; j++)
+                if (axis_conflict(B[ids[i]], B[ids[j]], a)) {
+                    int ra = find(i), rb = find(j);
+                    if (ra != rb)
+                        par[rb] = ra;
+                }
+        for (int i = 0; i < n; i++) {
+            int c = B[ids[i]].ent.empty() ? 1 : (int)B[ids[i]].ent.size();
+            sum[find(i)] += c;
+        }
+        for (int i = 0; i < n; i++) {
+            int c = B[ids[i]].ent.empty() ? 1 : (int)B[ids[i]].ent.size();
+            int t = (int)sum[find(i)];
+            coe[3 * i + a] = t > 0 ? (double)c / (double)t : 1.0;
+        }
+    }
+}
+
+// balance_parallel_sequences_for_gpu (block.cu:660-697) + the coe pass of
+// Preproccess_list (block.cu:1157)
+void balance(Schedule& s, int threads)
+{
+    const auto& B = s.blocks;
+    const int target = s.target;
+    std::vector<std::vector<int32_t>> groups;
+    for (size_t st = 0; st + 1 < s.strata_off.size(); st++) {
+        std::vector<int32_t> cur;
+        for (int32_t k = s.strata_off[st]; k < s.strata_off[st + 1]; k++) {
+            int32_t id = s.strata_ids[k];
+            if (B[id].ent.empty())
+                continue;
+            cur.push_back(id);
+            if ((int)cur.size() == target) {
+                groups.push_back(cur);
+                cur.clear();
+            }
+        }
+        if (!cur.empty())
+            groups.push_back(cur);
+    }
+    // candidates in (nnz, id) order: the first zero-score one is the answer
+    std::vector<int32_t> order;
+    for (int32_t i = 0; i < (int32_t)B.size(); i++)
+        if (!B[i].ent.empty())
+            order.push_back(i);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int32_t a, int32_t b) { return B[a].ent.size() < B[b].ent.size(); });
+
+    std::atomic<size_t> next(0);
+    auto worker = [&]() {
+        for (;;) {
+            size_t gi = next.fetch_add(1);
+            if (gi >= groups.size())
+                break;
+            std::vector<int32_t>& G = groups[gi];
+            while ((int)G.size() < target) {
+                int best = -1, best_score = 0;
+                for (int32_t c : order) {
+                    bool member = false;
+                    for (int32_t m : G)
+                        if (m == c) {
+                            member = true;
+                            break;
+                        }
+                    if (member)
+                        continue;
+                    const BlockRec& cb = B[c];
+                    int score = 0;
+                    bool pruned = false;
+                    for (int32_t m : G) {
+                        const BlockRec& mb = B[m];
+                        for (int a = 0; a < 3; a++)
+                            if ((mb.bins[a] & cb.bins[a]) && axis_conflict(mb, cb, a))
+                                score++;
+                        if (best >= 0 && score >= best_score) {
+                            pruned = true;
+                            break;
+                        }
+                    }
+                    if (pruned)
+                        continue;
+                    if (best < 0 || score < best_score) {
+                        best = c;
+                        best_score = score;
+                        if (score == 0)
+                            break;
+                    }
+                }
+                if (best < 0)
+                    break;
+                G.push_back(best);
+            }
+        }
+    };
+    int nt = std::max(1, std::min<int>(threads, (int)groups.size()));
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; t++)
+        pool.emplace_back(worker);
+    worker();
+    for (auto& t : pool)
+        t.join();
+
+    s.group_off.assign(1, 0);
+    s.slot_block.clear();
+    s.max_parallel = 0;
+    s.scheduled_updates = 0;
+    for (auto& G : groups) {
+        s.slot_block.insert(s.slot_block.end(), G.begin(), G.end());
+        s.group_off.push_back((int32_t)s.slot_block.size());
+        s.max_parallel = std::max<int32_t>(s.max_parallel, (int32_t)G.size());
+        for (int32_t b : G)
+            s.scheduled_updates += (int64_t)B[b].ent.size();
+    }
+    s.slot_coe.assign(3 * s.slot_block.size(), 1.0);
+    for (size_t gi = 0; gi + 1 < s.group_off.size(); gi++) {
+        int32_t o = s.group_off[gi];
+        coe_weights(B, s.slot_block.data() + o, s.group_off[gi + 1] - o, s.slot_coe.data() + 3 * (size_t)o);
+    }
+}
+
+}  // namespace
+
+int32_t stratum_target(int32_t max_parallel, int32_t block_num, int32_t pss, int32_t resident)
+{
+    int32_t target;
+    if (pss > 0) {
+        target = pss;
+    } else {
+        target = max_parallel > 0 ? max_parallel : 1;
+        if (resident > 0 && resident < target)
+            target = resident;
+        if (target < 1)
+            target = 1;
+        if (block_num > 0 && target > block_num)
+            target = block_num;
+    }
+    if (target < 1)
+        target = 1;
+    if (block_num > 0 && target > block_num)
+        target = block_num;
+    return target;
+}
+
+btc_status build_schedule(const btc_config& cfg, const int32_t* xyz, int64_t n, int resident,
+                          int threads, Schedule& s)
+{
+    if (n < 0 || n > 0x7fffffffLL || cfg.block_s <= 0 || cfg.I <= 0 || cfg.J <= 0 || cfg.K <= 0 ||
+        cfg.parallel_sequence_size < 0)
+        return BTC_ERR_ARG;
+    for (int64_t i = 0; i < 3 * n; i++) {
+        int d = (i % 3 == 0) ? cfg.I : (i % 3 == 1 ? cfg.J : cfg.K);
+        if (xyz[i] < 0 || xyz[i] >= d)
+            return BTC_ERR_RANGE;
+    }
+    s = Schedule();
+    s.I = cfg.I;
+    s.J = cfg.J;
+    s.K = cfg.K;
+    s.block_s = cfg.block_s;
+    s.pss = cfg.parallel_sequence_size;
+    s.train_nnz = n;
+    double t0 = now_s();
+    btc_status rc = blocking(xyz, n, cfg.I, cfg.J, cfg.K, cfg.block_s, s);
+    if (rc != BTC_OK)
+        return rc;
+    double t1 = now_s();
+    strata_first_fit(s);
+    double t2 = now_s();
+    s.target = stratum_target(s.max_parallel_cf, (int32_t)s.blocks.size(), s.pss, resident);
+    balance(s, threads);
+    double t3 = now_s();
+    s.seconds[0] = t1 - t0;
+    s.seconds[1] = t2 - t1;
+    s.seconds[2] = t3 - t2;
+    return BTC_OK;
+}
+
+namespace {
+// axis_range_to_string (block.cu:787-820): double-width ranges for the report
+std::string axis_range(const BlockRec& b, int a, int axis_size)
+{
+    std::ostringstream ss;
+    if (axis_size <= 0)
+        return "[]";
+    int levels = b.level[a] - 1;
+    if (levels <= 0 || levels >= 62) {
+        ss << "[0," << axis_size - 1 << "]";
+        return ss.str();
+    }
+    long long partitions = 1LL << levels;
+    long long code = (long long)b.code[a];
+    double width = (axis_size + 1.0) / partitions;
+    int begin = (int)std::floor(code * width);
+    int end = (int)std::floor((code + 1) * width) - 1;
+    if (begin < 0)
+        begin = 0;
+    if (begin >= axis_size)
+        begin = axis_size - 1;
+    if (end < begin)
+        end = begin;
+    if (end >= axis_size)
+        end = axis_size - 1;
+    ss << "[" << begin << "," << end << "]";
+    return ss.str();
+}
+
+std::string id_string(const BlockRec& b, int a)
+{
+    std::string r(1, '0');
+    for (int k = b.level[a] - 2; k >= 0; k--)
+        r += ((b.code[a] >> k) & 1ULL) ? '1' : '0';
+    return r;
+}
+
+struct Stats {
+    int count = 0, minv = 0, maxv = 0, scheduled = 0, unique = 0;
+};
+
+Stats stats_of(const std::vector<int32_t>& off, const std::vector<int32_t>& ids)
+{
+    Stats st;
+    std::set<int32_t> u;
+    for (size_t g = 0; g + 1 < off.size(); g++) {
+        int sz = off[g + 1] - off[g];
+        if (sz == 0)
+            continue;
+        st.count++;
+        st.scheduled += sz;
+        if (st.minv == 0 || sz < st.minv)
+            st.minv = sz;
+        st.maxv = std::max(st.maxv, sz);
+        for (int k = off[g]; k < off[g + 1]; k++)
+            u.insert(ids[k]);
+    }
+    st.unique = (int)u.size();
+    return st;
+}
+}  // namespace
+
+std::string report_text(const Schedule& s)
+{
+    std::ostringstream o;
+    int ngroups = (int)s.group_off.size() - 1;
+    int num_parallel = ngroups + 1;
+    int non_empty = 0;
+    for (const auto& b : s.blocks)
+        non_empty += b.ent.empty() ? 0 : 1;
+    Stats cf = stats_of(s.strata_off, s.strata_ids);
+    Stats ac = stats_of(s.group_off, s.slot_block);
+    o << "# block_s " << s.block_s << "\n";
+    o << "# parallel_sequence_size " << (s.pss > 0 ? s.pss : 0) << " (0 means auto)\n";
+    o << "# num_block_total " << s.blocks.size() << "\n";
+    o << "# non_empty_blocks " << non_empty << "\n";
+    o << "# num_parallel_nodes " << num_parallel << "\n";
+    o << "# scheduled_blocks " << ac.scheduled << "\n";
+    o << "# unique_scheduled_blocks " << ac.unique << "\n";
+    o << "# max_sequence_size " << ac.maxv << "\n";
+    o << "# target_gpu_blocks " << s.target << "\n";
+    o << "# conflict_free_sequence_count " << cf.count << "\n";
+    o << "# conflict_free_min_parallel_blocks " << cf.minv << "\n";
+    o << "# conflict_free_max_parallel_blocks " << cf.maxv << "\n";
+    o << "# conflict_free_scheduled_blocks " << cf.scheduled << "\n";
+    o << "# conflict_free_unique_blocks " << cf.unique << "\n";
+    o << "# after_conflict_sequence_count " << ac.count << "\n";
+    o << "# after_conflict_min_parallel_blocks " << ac.minv << "\n";
+    o << "# after_conflict_max_parallel_blocks " << ac.maxv << "\n";
+    o << "# after_conflict_scheduled_blocks " << ac.scheduled << "\n";
+    o << "# after_conflict_unique_blocks " << ac.unique << "\n";
+    o << "\n";
+    o << "[blocks]\n";
+    o << "block_id nnz level_x level_y level_z x_id x_range y_id y_range z_id z_range\n";
+    const int dims[3] = {s.I, s.J, s.K};
+    for (size_t i = 0; i < s.blocks.size(); i++) {
+        const BlockRec& b = s.blocks[i];
+        if (b.ent.empty())
+            continue;
+        o << i << ' ' << b.ent.size() << ' ' << b.level[0] << ' ' << b.level[1] << ' ' << b.level[2];
+        for (int a = 0; a < 3; a++)
+            o << ' ' << id_string(b, a) << ' ' << axis_range(b, a, dims[a]);
+        o << "\n";
+    }
+    o << "\n";
+    o << "[parallel_sequences]\n";
+    o << "sequence_id size total_nnz block_ids\n";
+    int seq = 0;
+    for (int g = 0; g < ngroups; g++) {
+        int a = s.group_off[g], e = s.group_off[g + 1];
+        if (a == e)
+            continue;
+        long long tot = 0;
+        for (int k = a; k < e; k++)
+            tot += (long long)s.blocks[s.slot_block[k]].ent.size();
+        o << seq << ' ' << (e - a) << ' ' << (int)tot << ' ';
+        for (int k = a; k < e; k++) {
+            if (k > a)
+                o << ',';
+            o << s.slot_block[k];
+        }
+        o << "\n";
+        seq++;
+    }
+    return o.str();
+}
+
+}  // namespace btc

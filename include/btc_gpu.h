@@ -1,0 +1,224 @@
+/*
+ * btc_gpu.h -- C ABI of the GB300-native BTC-GPU sparse CP-SGD path.
+ *
+ * The reference reaches its GPU code through three C++ seams with config in
+ * mutable globals:
+ *   tensor_SGD(train, test)                       tensor_SGD.h:101, tensor_SGD.cu:55-90
+ *   block_problem(train, n, test, m, a, b, c, rate)   block.h:24-31,  block.cu:1233-1287
+ *   sgd_train(train, n, test, m, a, b, c, num_parallel, max_parallel, ..., num_bs, bs, nbs)
+ *                                                 sgd_Kernel.h:24-38, sgd_Kernel.cu:968-1361
+ * This header replaces them with plain C entry points: a config struct in
+ * place of the globals, a host-side schedule object in place of block_problem's
+ * BS_node/b_node arrays, and a device context in place of sgd_train's body.
+ * All pointers are caller-owned host memory unless stated; nothing here
+ * exits the process: every call returns a btc_status.
+ *
+ * Layout conventions:
+ *   coordinates  int32 triples (x, y, z), 0-based, row-major n x 3
+ *   values       double (the reference's T_node::rate, tensor_SGD.h:52-55)
+ *   factors      row-major [rows][rank] double on the host side; the device
+ *                copy is stored in the context's dtype
+ */
+#ifndef BTC_GPU_H
+#define BTC_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BTC_ABI_VERSION 1
+
+typedef enum btc_status {
+    BTC_OK = 0,
+    BTC_ERR_ARG = 1,         /* invalid argument or configuration */
+    BTC_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    BTC_ERR_ALLOC = 3,       /* host or device allocation failed */
+    BTC_ERR_STATE = 4,       /* call out of order / object in a failed state */
+    BTC_ERR_IO = 5,          /* file could not be opened, read or written */
+    BTC_ERR_TIMEOUT = 6,     /* a bounded device wait gave up */
+    BTC_ERR_UNSUPPORTED = 7, /* valid request this build does not implement */
+    BTC_ERR_RANGE = 8,       /* index or level outside the representable range */
+    BTC_ERR_NO_DEVICE = 9,   /* no CUDA device visible */
+    BTC_ERR_DEVICE = 10      /* a kernel reported an error status */
+} btc_status;
+
+typedef enum btc_dtype {
+    BTC_DTYPE_F32 = 0,  /* FP32 factors, FP32 math (the plain path) */
+    BTC_DTYPE_F64 = 1,  /* FP64 factors and math (the reference's precision) */
+    BTC_DTYPE_BF16 = 2  /* BF16 factors, FP32 math, stochastic rounding */
+} btc_dtype;
+
+typedef enum btc_mode {
+    /* Every slot of the schedule is cut into chunks that all SMs sweep in
+     * schedule order; rows are read from L2 and updated with atomic adds,
+     * as the reference's GPUs kernel does inside a slot. Not bit-reproducible. */
+    BTC_MODE_HOGWILD = 0,
+    /* Slots run one warp each, entries strictly in block order, and slots that
+     * share a factor row run in schedule order.  Bit-identical to a serial
+     * replay of the schedule (the FP64 instantiation matches the serial FP64
+     * rule bit for bit). */
+    BTC_MODE_DETERMINISTIC = 1,
+    /* One CTA per slot: the slot's reused rows are staged in shared memory,
+     * updated there, and each row is written back once as a delta. */
+    BTC_MODE_STAGED = 2
+} btc_mode;
+
+typedef enum btc_split { BTC_SPLIT_TRAIN = 0, BTC_SPLIT_TEST = 1 } btc_split;
+
+/* Configuration: the reference's globals (tensor_SGD.h:25-42, defaults in
+ * tensor_SGD.cu:24-41) plus the options this build adds. */
+typedef struct btc_config {
+    int32_t I, J, K;                /* mode sizes */
+    int32_t epochs;                 /* default 1000 */
+    int32_t rank;                   /* r, default 16 */
+    double lr;                      /* default 0.005 */
+    double reg;                     /* default 0.0005 */
+    int32_t block_s;                /* block capacity, default 2048 */
+    int32_t thread_size;            /* accepted for compatibility, default 512 */
+    int32_t parallel_sequence_size; /* blocks per stratum on the GPU; 0 = auto; default 8 */
+    int32_t requested_gpu_count;    /* accepted; this build always uses one GPU */
+    int32_t dtype;                  /* btc_dtype, default BTC_DTYPE_F32 */
+    int32_t mode;                   /* btc_mode, default BTC_MODE_HOGWILD */
+    int32_t device;                 /* CUDA device ordinal, default 0 */
+    /* SMs x max resident blocks per SM used by the auto stratum width
+     * (block.cu:577-606); 0 = ask the device, -1 = no device (width =
+     * widest conflict-free stratum) */
+    int32_t resident_blocks;
+    int32_t chunk;                  /* entries per Hogwild work item, 0 = auto */
+    int32_t host_threads;           /* builder threads, 0 = hardware concurrency */
+    int32_t reserved[7];
+} btc_config;
+
+typedef struct btc_schedule_summary {
+    int32_t num_blocks;          /* blocks created, including empty ones */
+    int32_t nonempty_blocks;
+    int32_t num_strata;          /* conflict-free strata before balancing */
+    int32_t max_parallel_cf;     /* widest conflict-free stratum */
+    int32_t target_gpu_blocks;   /* stratum width after balancing */
+    int32_t num_groups;          /* strata after balancing (num_parallel - 1) */
+    int32_t num_slots;           /* scheduled (block, stratum) pairs */
+    int32_t max_parallel;        /* widest balanced stratum (the reference's grid size) */
+    int64_t scheduled_updates;   /* entries executed per epoch (sum of slot nnz) */
+    int64_t train_nnz;
+    int32_t global_levels[3];    /* final global split level per axis */
+    int32_t reserved;
+    double build_seconds[3];     /* blocking, strata, balancing wall time */
+} btc_schedule_summary;
+
+typedef struct btc_metrics {
+    double rmse, mae, er;        /* compute_metrics_gpu's outputs (sgd_Kernel.cu:136-201) */
+    double sse, sae, ref2;       /* FP64 sums they are derived from */
+    int64_t count;
+} btc_metrics;
+
+typedef struct btc_epoch_stats {
+    double kernel_ms;            /* device time of the epoch's SGD launches (CUDA events) */
+    int64_t updates;             /* entries executed */
+    int32_t launches;            /* kernels launched for the epoch */
+    int32_t device_status;       /* error word the kernels wrote (0 = none) */
+} btc_epoch_stats;
+
+typedef struct btc_schedule btc_schedule;
+typedef struct btc_ctx btc_ctx;
+
+const char *btc_status_string(btc_status s);
+int32_t btc_abi_version(void);
+
+/* Reference defaults (tensor_SGD.cu:24-41). */
+btc_status btc_config_default(btc_config *cfg);
+/* Validation as main.cpp:169-203 (rank in [1,100] lifted to [1,128]). */
+btc_status btc_config_validate(const btc_config *cfg);
+
+/* ---- text I/O (main.cpp:24-99) ------------------------------------------
+ * Reads "x y z value" lines; skips empty lines, lines starting with '#' or
+ * '%', and lines that do not start with three integers and a number;
+ * subtracts coord_base; rejects out-of-range coordinates with BTC_ERR_RANGE
+ * (the reference exits).  The arrays are allocated by the library and freed
+ * with btc_free; *line_no receives the offending line on BTC_ERR_RANGE. */
+btc_status btc_read_entries(const char *path, int32_t coord_base, int32_t I, int32_t J,
+                            int32_t K, int32_t **xyz, double **val, int64_t *n,
+                            int64_t *line_no);
+void btc_free(void *p);
+/* std::shuffle with std::mt19937(seed) over n entries, as main.cpp:303-306
+ * does with seed 42; permutes xyz and val together. */
+btc_status btc_shuffle_entries(int32_t *xyz, double *val, int64_t n, uint32_t seed);
+
+/* ---- host schedule (replaces block_problem up to Preproccess_list,
+ *      block.cu:1233-1278) ------------------------------------------------ */
+btc_status btc_schedule_build(const btc_config *cfg, const int32_t *xyz, int64_t n,
+                              btc_schedule **out);
+btc_status btc_schedule_summarize(const btc_schedule *s, btc_schedule_summary *out);
+/* per block: meta[4*b..] = nnz, level_x, level_y, level_z; codes[3*b+a] =
+ * id bits 1..level-1 of axis a, MSB first (position 0 is always 0) */
+btc_status btc_schedule_blocks(const btc_schedule *s, int32_t *meta, uint64_t *codes);
+/* entry indices (into the array given to btc_schedule_build) of block b, in
+ * block order; *n in: capacity, out: count */
+btc_status btc_schedule_block_entries(const btc_schedule *s, int32_t b, int32_t *out,
+                                      int32_t *n);
+/* conflict-free strata before balancing: off[num_strata+1], ids[] */
+btc_status btc_schedule_strata(const btc_schedule *s, int32_t *off, int32_t *ids);
+/* balanced groups: off[num_groups+1], slot block ids, coe[3*slot] */
+btc_status btc_schedule_groups(const btc_schedule *s, int32_t *off, int32_t *slot_block,
+                               double *slot_coe);
+/* block_parallel.txt, byte-compatible with block.cu:822-925 */
+btc_status btc_schedule_write_report(const btc_schedule *s, const btc_config *cfg,
+                                     const char *path);
+void btc_schedule_free(btc_schedule *s);
+
+/* ---- device context (replaces sgd_train's state, sgd_Kernel.cu:1042-1266) */
+btc_status btc_ctx_create(const btc_config *cfg, const btc_schedule *s, const int32_t *train_xyz,
+                          const double *train_val, int64_t ntrain, const int32_t *test_xyz,
+                          const double *test_val, int64_t ntest, btc_ctx **out);
+/* mode 0 = A (I rows), 1 = B (J rows), 2 = C (K rows); host is [rows][rank] */
+btc_status btc_ctx_set_factors(btc_ctx *ctx, int32_t mode, const double *host);
+btc_status btc_ctx_get_factors(btc_ctx *ctx, int32_t mode, double *host);
+/* U(lo, hi) init from a counter-based generator (seed, mode, row, col) */
+btc_status btc_ctx_init_factors(btc_ctx *ctx, uint64_t seed, double lo, double hi);
+/* One epoch: the reference's GPUs<<<max_parallel, thread_size>>> launch
+ * (sgd_Kernel.cu:1283-1285). */
+btc_status btc_train_epoch(btc_ctx *ctx, btc_epoch_stats *stats);
+/* n epochs back to back on the context's stream, bracketed by CUDA events on
+ * that stream; stats->kernel_ms is the device time of all n epochs. */
+btc_status btc_train_epochs(btc_ctx *ctx, int32_t n, btc_epoch_stats *stats);
+/* compute_metrics_gpu (sgd_Kernel.cu:136-201) on the train or test split;
+ * FP64 sums on the GPU.  count 0 gives NaN metrics like the reference. */
+btc_status btc_eval(btc_ctx *ctx, int32_t split, btc_metrics *out);
+/* Device stream the context launches on (a cudaStream_t). */
+void *btc_ctx_stream(btc_ctx *ctx);
+btc_status btc_ctx_destroy(btc_ctx *ctx);
+
+/* One end-to-end step from host buffers: upload the factors, run one epoch,
+ * evaluate the test split and read the factors back (the timed unit of the
+ * end-to-end measurement). */
+btc_status btc_train_epoch_host(btc_ctx *ctx, double *A, double *B, double *C,
+                                btc_epoch_stats *stats, btc_metrics *test);
+
+/* Page-locked host memory for the end-to-end transfers (cudaHostAlloc). */
+btc_status btc_host_alloc(void **p, int64_t bytes);
+void btc_host_free(void *p);
+
+/* ---- synthetic tensors ---------------------------------------------------- */
+typedef struct btc_gen_spec {
+    int32_t I, J, K;
+    int64_t nnz;               /* unique entries to produce */
+    double zipf_s[3];          /* per mode; 0 = uniform */
+    int32_t gt_rank;           /* ground-truth CP rank (values), 0 = log-normal values */
+    double gt_std;             /* ground-truth factor std */
+    double noise_std;
+    double train_frac;         /* Bernoulli train probability */
+    uint64_t seed;
+    int32_t threads;           /* 0 = hardware concurrency */
+    int32_t reserved[3];
+} btc_gen_spec;
+
+/* Library-allocated arrays (free with btc_free). */
+btc_status btc_gen_tensor(const btc_gen_spec *spec, int32_t **train_xyz, double **train_val,
+                          int64_t *ntrain, int32_t **test_xyz, double **test_val,
+                          int64_t *ntest);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BTC_GPU_H */

@@ -716,3 +716,164 @@ void orc_metrics(const int32_t *xyz, const double *val, int64_t n, int R, const 
 
 /* Expose hx for the tests of the float-rounding quirk. */
 int orc_hx_public(int end, int level, int num, int64_t *out) { return orc_hx(end, level, num, out); }
+
+/* ---- replay over a flattened schedule ----------------------------------
+ * slot k covers entry indices ent[soff[k] .. soff[k+1]) of xyz/val and has
+ * weights coe[3k..3k+2]; slots [s0, s1) are replayed in order.  This is the
+ * serial CPU baseline of the reference update rule (sgd_Kernel.cu:336-351). */
+int64_t orc_sgd_replay(int64_t s0, int64_t s1, const int64_t *soff, const int32_t *ent,
+                       const double *coe, const int32_t *xyz, const double *val, int R, double lr,
+                       double reg, double *A, double *B, double *C)
+{
+    int64_t upd = 0;
+    double av[256], bv[256], cv[256];
+    if (R > 256)
+        return -1;
+    for (int64_t k = s0; k < s1; k++) {
+        double cx = coe[3 * k] * lr, cy = coe[3 * k + 1] * lr, cz = coe[3 * k + 2] * lr;
+        for (int64_t t = soff[k]; t < soff[k + 1]; t++) {
+            int e = ent[t];
+            double *Ar = A + (size_t)xyz[3 * (int64_t)e] * R;
+            double *Br = B + (size_t)xyz[3 * (int64_t)e + 1] * R;
+            double *Cr = C + (size_t)xyz[3 * (int64_t)e + 2] * R;
+            double dot = 0.0;
+            for (int q = 0; q < R; q++) {
+                av[q] = Ar[q];
+                bv[q] = Br[q];
+                cv[q] = Cr[q];
+                dot = fma(av[q], bv[q] * cv[q], dot);
+            }
+            double err = val[e] - dot;
+            for (int q = 0; q < R; q++) {
+                Ar[q] = Ar[q] + cx * (err * (bv[q] * cv[q]) - reg * av[q]);
+                Br[q] = Br[q] + cy * (err * (av[q] * cv[q]) - reg * bv[q]);
+                Cr[q] = Cr[q] + cz * (err * (av[q] * bv[q]) - reg * cv[q]);
+            }
+            upd++;
+        }
+    }
+    return upd;
+}
+
+/* Multi-threaded replay: the entries of one group (stratum) are split
+ * across threads that read rows and add deltas with atomic compare-and-swap,
+ * the reference GPU kernel's Hogwild model on host cores; a barrier separates
+ * groups.  Groups [g0, g1) of goff[] (slot offsets per group). */
+#include <pthread.h>
+
+typedef struct {
+    int tid, nthreads;
+    int64_t g0, g1;
+    const int64_t *goff, *soff;
+    const int32_t *ent;
+    const double *coe;
+    const int32_t *xyz;
+    const double *val;
+    int R;
+    double lr, reg;
+    double *A, *B, *C;
+    pthread_barrier_t *bar;
+    int64_t upd;
+} orc_mt_arg;
+
+static double ld_relaxed(const double *p)
+{
+    uint64_t u = __atomic_load_n((const uint64_t *)p, __ATOMIC_RELAXED);
+    double d;
+    memcpy(&d, &u, 8);
+    return d;
+}
+
+static void add_atomic(double *p, double v)
+{
+    uint64_t *u = (uint64_t *)p;
+    uint64_t old = __atomic_load_n(u, __ATOMIC_RELAXED), nw;
+    do {
+        double d;
+        memcpy(&d, &old, 8);
+        d = d + v;
+        memcpy(&nw, &d, 8);
+    } while (!__atomic_compare_exchange_n(u, &old, nw, 1, __ATOMIC_RELAXED, __ATOMIC_RELAXED));
+}
+
+static void *orc_mt_worker(void *vp)
+{
+    orc_mt_arg *a = (orc_mt_arg *)vp;
+    double av[256], bv[256], cv[256];
+    int R = a->R;
+    for (int64_t g = a->g0; g < a->g1; g++) {
+        int64_t s0 = a->goff[g], s1 = a->goff[g + 1];
+        int64_t e0 = a->soff[s0], e1 = a->soff[s1];
+        int64_t n = e1 - e0;
+        int64_t lo = e0 + n * a->tid / a->nthreads, hi = e0 + n * (a->tid + 1) / a->nthreads;
+        int64_t k = s0;
+        for (int64_t t = lo; t < hi; t++) {
+            while (a->soff[k + 1] <= t)
+                k++;
+            double cx = a->coe[3 * k] * a->lr, cy = a->coe[3 * k + 1] * a->lr, cz = a->coe[3 * k + 2] * a->lr;
+            int e = a->ent[t];
+            double *Ar = a->A + (size_t)a->xyz[3 * (int64_t)e] * R;
+            double *Br = a->B + (size_t)a->xyz[3 * (int64_t)e + 1] * R;
+            double *Cr = a->C + (size_t)a->xyz[3 * (int64_t)e + 2] * R;
+            double dot = 0.0;
+            for (int q = 0; q < R; q++) {
+                av[q] = ld_relaxed(Ar + q);
+                bv[q] = ld_relaxed(Br + q);
+                cv[q] = ld_relaxed(Cr + q);
+                dot = fma(av[q], bv[q] * cv[q], dot);
+            }
+            double err = a->val[e] - dot;
+            for (int q = 0; q < R; q++) {
+                add_atomic(Ar + q, cx * (err * (bv[q] * cv[q]) - a->reg * av[q]));
+                add_atomic(Br + q, cy * (err * (av[q] * cv[q]) - a->reg * bv[q]));
+                add_atomic(Cr + q, cz * (err * (av[q] * bv[q]) - a->reg * cv[q]));
+            }
+            a->upd++;
+        }
+        pthread_barrier_wait(a->bar);
+    }
+    return NULL;
+}
+
+int64_t orc_sgd_replay_mt(int64_t g0, int64_t g1, const int64_t *goff, const int64_t *soff,
+                          const int32_t *ent, const double *coe, const int32_t *xyz, const double *val,
+                          int R, double lr, double reg, double *A, double *B, double *C, int threads)
+{
+    if (threads < 1 || threads > 512 || R > 256)
+        return -1;
+    pthread_t th[512];
+    orc_mt_arg args[512];
+    pthread_barrier_t bar;
+    pthread_barrier_init(&bar, NULL, (unsigned)threads);
+    for (int t = 0; t < threads; t++) {
+        orc_mt_arg *a = &args[t];
+        a->tid = t;
+        a->nthreads = threads;
+        a->g0 = g0;
+        a->g1 = g1;
+        a->goff = goff;
+        a->soff = soff;
+        a->ent = ent;
+        a->coe = coe;
+        a->xyz = xyz;
+        a->val = val;
+        a->R = R;
+        a->lr = lr;
+        a->reg = reg;
+        a->A = A;
+        a->B = B;
+        a->C = C;
+        a->bar = &bar;
+        a->upd = 0;
+    }
+    for (int t = 1; t < threads; t++)
+        pthread_create(&th[t], NULL, orc_mt_worker, &args[t]);
+    orc_mt_worker(&args[0]);
+    int64_t upd = args[0].upd;
+    for (int t = 1; t < threads; t++) {
+        pthread_join(th[t], NULL);
+        upd += args[t].upd;
+    }
+    pthread_barrier_destroy(&bar);
+    return upd;
+}

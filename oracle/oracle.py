@@ -45,6 +45,12 @@ def _load():
     lib.orc_sgd_epoch.argtypes = [P, P, P, ctypes.c_int, ctypes.c_double, ctypes.c_double, P, P, P]
     lib.orc_sgd_epoch.restype = ctypes.c_int64
     lib.orc_metrics.argtypes = [P, P, ctypes.c_int64, ctypes.c_int, P, P, P, P]
+    lib.orc_sgd_replay.argtypes = [ctypes.c_int64, ctypes.c_int64, P, P, P, P, P, ctypes.c_int,
+                                   ctypes.c_double, ctypes.c_double, P, P, P]
+    lib.orc_sgd_replay.restype = ctypes.c_int64
+    lib.orc_sgd_replay_mt.argtypes = [ctypes.c_int64, ctypes.c_int64, P, P, P, P, P, P, ctypes.c_int,
+                                      ctypes.c_double, ctypes.c_double, P, P, P, ctypes.c_int]
+    lib.orc_sgd_replay_mt.restype = ctypes.c_int64
     lib.orc_hx_public.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
     lib.orc_hx_public.restype = ctypes.c_int
     _lib = lib
@@ -150,3 +156,42 @@ def hx(end, level, num):
     if rc:
         raise OverflowError("hx out of range")
     return int(out[0])
+
+
+class FlatSchedule:
+    """A schedule given as flat arrays (groups -> slots -> entry indices), for
+    replaying the reference update rule on host cores (the CPU baseline)."""
+
+    def __init__(self, group_off, slot_blocks, slot_coe, block_entries):
+        self.goff = np.ascontiguousarray(group_off, np.int64)
+        sizes = np.array([len(block_entries(int(b))) for b in slot_blocks], np.int64)
+        self.soff = np.zeros(len(slot_blocks) + 1, np.int64)
+        np.cumsum(sizes, out=self.soff[1:])
+        cache = {}
+        parts = []
+        for b in slot_blocks:
+            b = int(b)
+            if b not in cache:
+                cache[b] = np.asarray(block_entries(b), np.int32)
+            parts.append(cache[b])
+        self.ent = np.ascontiguousarray(np.concatenate(parts) if parts else np.zeros(0, np.int32))
+        self.coe = np.ascontiguousarray(slot_coe, np.float64)
+        self.nslots = len(slot_blocks)
+        self.ngroups = len(self.goff) - 1
+
+    def replay(self, xyz, val, R, lr, reg, A, B, C, s0=0, s1=None):
+        lib = _load()
+        s1 = self.nslots if s1 is None else s1
+        xyz = np.ascontiguousarray(xyz, np.int32)
+        val = np.ascontiguousarray(val, np.float64)
+        return lib.orc_sgd_replay(s0, s1, _ptr(self.soff), _ptr(self.ent), _ptr(self.coe), _ptr(xyz),
+                                  _ptr(val), R, lr, reg, _ptr(A), _ptr(B), _ptr(C))
+
+    def replay_mt(self, xyz, val, R, lr, reg, A, B, C, threads, g0=0, g1=None):
+        lib = _load()
+        g1 = self.ngroups if g1 is None else g1
+        xyz = np.ascontiguousarray(xyz, np.int32)
+        val = np.ascontiguousarray(val, np.float64)
+        return lib.orc_sgd_replay_mt(g0, g1, _ptr(self.goff), _ptr(self.soff), _ptr(self.ent),
+                                     _ptr(self.coe), _ptr(xyz), _ptr(val), R, lr, reg, _ptr(A), _ptr(B),
+                                     _ptr(C), threads)
