@@ -654,6 +654,36 @@ btc_status btc_train_epochs(btc_ctx* c, int32_t n, btc_epoch_stats* st)
     return BTC_OK;
 }
 
+btc_status btc_device_count(int32_t* count)
+{
+    if (!count)
+        return BTC_ERR_ARG;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+        *count = 0;
+        cuda_fail(e, "cudaGetDeviceCount");
+        return e == cudaErrorNoDevice ? BTC_ERR_NO_DEVICE : BTC_ERR_CUDA;
+    }
+    *count = n;
+    return BTC_OK;
+}
+
+btc_status btc_device_info(int32_t device, char* name, int32_t* sm_count, int64_t* memory_bytes)
+{
+    cudaDeviceProp p;
+    CK(cudaGetDeviceProperties(&p, device));
+    if (name) {
+        std::strncpy(name, p.name, 255);
+        name[255] = 0;
+    }
+    if (sm_count)
+        *sm_count = p.multiProcessorCount;
+    if (memory_bytes)
+        *memory_bytes = (int64_t)p.totalGlobalMem;
+    return BTC_OK;
+}
+
 btc_status btc_host_alloc(void** p, int64_t bytes)
 {
     if (!p || bytes < 0)

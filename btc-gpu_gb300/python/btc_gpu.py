@@ -97,6 +97,8 @@ SIGNATURES = {
     "btc_train_epochs": ([P, I32, P], ctypes.c_int),
     "btc_eval": ([P, I32, P], ctypes.c_int),
     "btc_host_alloc": ([P, I64], ctypes.c_int),
+    "btc_device_count": ([P], ctypes.c_int),
+    "btc_device_info": ([I32, ctypes.c_char_p, P, P], ctypes.c_int),
     "btc_host_free": ([P], None),
     "btc_ctx_stream": ([P], P),
     "btc_ctx_destroy": ([P], ctypes.c_int),

@@ -195,6 +195,11 @@ btc_status btc_ctx_destroy(btc_ctx *ctx);
 btc_status btc_train_epoch_host(btc_ctx *ctx, double *A, double *B, double *C,
                                 btc_epoch_stats *stats, btc_metrics *test);
 
+/* Visible CUDA devices (main.cpp:274-284 and the inventory of
+ * sgd_Kernel.cu:492-503); name must hold 256 bytes. */
+btc_status btc_device_count(int32_t *count);
+btc_status btc_device_info(int32_t device, char *name, int32_t *sm_count, int64_t *memory_bytes);
+
 /* Page-locked host memory for the end-to-end transfers (cudaHostAlloc). */
 btc_status btc_host_alloc(void **p, int64_t bytes);
 void btc_host_free(void *p);
