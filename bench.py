@@ -56,6 +56,7 @@ WORKLOADS = {
 }
 METRIC = "nnz-updates/s & time-to-test-RMSE, tuned vs plain FP32, 1×GB300, % HBM peak"
 SEED = 20261203 + 1
+CTAS = 0
 
 
 def log(*a):
@@ -139,7 +140,7 @@ def cfg_for(w, dtype, mode, device=0):
     import btc_gpu as bg
 
     return bg.config(I=w["I"], J=w["J"], K=w["K"], rank=w["R"], lr=w["lr"], reg=w["reg"], block_s=2048,
-                     parallel_sequence_size=8, dtype=dtype, mode=mode, device=device)
+                     parallel_sequence_size=8, dtype=dtype, mode=mode, device=device, ctas_per_sm=CTAS)
 
 
 def flat_schedule(sched):
@@ -287,7 +288,7 @@ def run_gpu(args):
     achieved = b_upd * upd_per_launch / (per_launch_ms / 1000.0) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": None, "peak_source": src, "bytes_per_update": b_upd,
-                "kernel": "k_hogwild" if mode == bg.HOGWILD else "k_det"}
+                "kernel": {bg.HOGWILD: "k_hogwild", bg.STAGED: "k_staged"}.get(mode, "k_det")}
 
     line = None
     if rank == 0:
@@ -331,7 +332,10 @@ def main():
     ap.add_argument("--dtype", default="f32", choices=["f32", "f64", "bf16"])
     ap.add_argument("--mode", default="hogwild", choices=["hogwild", "deterministic", "staged"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ctas", type=int, default=0, help="staged kernel CTAs per SM (0 = auto)")
     args = ap.parse_args()
+    global CTAS
+    CTAS = args.ctas
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     if args.impl == "reference":
         return run_reference(args)

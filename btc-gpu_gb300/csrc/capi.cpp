@@ -31,6 +31,8 @@
 #include "common.h"
 #include "kernels.h"
 #include "schedule.h"
+#include "staged.h"
+#include "tiles.h"
 
 struct btc_schedule {
     btc::Schedule s;
@@ -59,6 +61,18 @@ struct btc_ctx {
     double* staging = nullptr;  // double [max rows][R] for factor transfers
     int* wave_slots = nullptr;
     std::vector<int> wave_off;
+    // staged mode
+    btc::TileHdr* tiles = nullptr;
+    int* slot_tile0 = nullptr;
+    int* slot_ntiles = nullptr;
+    int4* tent = nullptr;
+    unsigned short* tcsr = nullptr;
+    int4* tsegs = nullptr;
+    int* trows = nullptr;
+    double* tval64 = nullptr;
+    int* counter = nullptr;
+    int st_cap = 0, st_wave = 0, st_grid = 0, st_block = 256;
+    long long st_rows = 0, st_tiles = 0;
     int64_t updates = 0;
     int nslots = 0;
     bool failed = false;
@@ -311,6 +325,15 @@ btc_status btc_ctx_destroy(btc_ctx* c)
     free_dev(c->result);
     free_dev(c->staging);
     free_dev(c->wave_slots);
+    free_dev(c->tiles);
+    free_dev(c->slot_tile0);
+    free_dev(c->slot_ntiles);
+    free_dev(c->tent);
+    free_dev(c->tcsr);
+    free_dev(c->tsegs);
+    free_dev(c->trows);
+    free_dev(c->tval64);
+    free_dev(c->counter);
     if (c->ev0)
         cudaEventDestroy(c->ev0);
     if (c->ev1)
@@ -342,7 +365,7 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
     CK(cudaEventCreate(&c->ev1));
     c->dtype = cfg.dtype;
     c->mode = cfg.mode;
-    if (c->dtype == BTC_DTYPE_BF16 || c->mode == BTC_MODE_STAGED)
+    if (c->dtype == BTC_DTYPE_BF16)
         return BTC_ERR_UNSUPPORTED;
     c->esize = c->dtype == BTC_DTYPE_F64 ? 8 : 4;
     c->R = cfg.rank;
@@ -448,6 +471,48 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
 
     int occ = btc::hogwild_blocks_per_sm(c->dtype, c->R, c->hw_block);
     c->hw_grid = c->sms * std::max(1, occ);
+
+    if (c->mode == BTC_MODE_STAGED) {
+        c->st_wave = std::max(1, std::min(cfg.thread_size, 4096));
+        int ctas = cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 2;
+        c->st_cap = btc::staged_cap_for(c->dtype, c->Rp, c->st_wave, ctas, prop.sharedMemPerMultiprocessor,
+                                        prop.sharedMemPerBlockOptin);
+        if (c->st_cap < 3)
+            return BTC_ERR_UNSUPPORTED;  // one entry needs three staged rows
+        btc::TileSet ts;
+        btc::build_tiles(s, txyz, tval, cfg.I, cfg.J, cfg.K, c->st_cap, c->st_wave, 16,
+                         c->dtype == BTC_DTYPE_F64, ts);
+        std::vector<int> t0(nslots), tn(nslots);
+        for (int k = 0; k < nslots; k++) {
+            t0[k] = ts.block_tile0[(size_t)s.slot_block[k]];
+            tn[k] = ts.block_ntiles[(size_t)s.slot_block[k]];
+        }
+        c->st_tiles = (long long)ts.tiles.size();
+        c->st_rows = (long long)ts.rows.size();
+        if ((rc = upload((void**)&c->tiles, ts.tiles.data(), ts.tiles.size() * sizeof(btc::TileHdr), c->stream)))
+            return rc;
+        if ((rc = upload((void**)&c->slot_tile0, t0.data(), t0.size() * 4, c->stream)))
+            return rc;
+        if ((rc = upload((void**)&c->slot_ntiles, tn.data(), tn.size() * 4, c->stream)))
+            return rc;
+        if ((rc = upload((void**)&c->tent, ts.ent.data(), ts.ent.size() * sizeof(int4), c->stream)))
+            return rc;
+        if ((rc = upload((void**)&c->tcsr, ts.csr.data(), ts.csr.size() * 2, c->stream)))
+            return rc;
+        if ((rc = upload((void**)&c->tsegs, ts.segs.data(), ts.segs.size() * sizeof(int4), c->stream)))
+            return rc;
+        if ((rc = upload((void**)&c->trows, ts.rows.data(), ts.rows.size() * 4, c->stream)))
+            return rc;
+        if (!ts.val64.empty() && (rc = upload((void**)&c->tval64, ts.val64.data(), ts.val64.size() * 8, c->stream)))
+            return rc;
+        CK(cudaMalloc((void**)&c->counter, sizeof(int)));
+        size_t smem = btc::staged_smem_bytes(c->dtype, c->Rp, c->st_cap, c->st_wave);
+        int occ = btc::staged_blocks_per_sm(c->dtype, c->R, c->st_block, smem);
+        if (occ <= 0)
+            return BTC_ERR_UNSUPPORTED;
+        c->st_grid = c->sms * occ;
+        CK(cudaStreamSynchronize(c->stream));  // host tile arrays go out of scope
+    }
 
     if (c->mode == BTC_MODE_DETERMINISTIC) {
         // slots that share any factor row run in schedule order; the others
@@ -596,6 +661,32 @@ static btc_status enqueue_epoch(btc_ctx* c, int* launches)
             int b = c->wave_off[w], e = c->wave_off[w + 1];
             CK(btc::launch_det_wave(c->dtype, c->wave_slots + b, e - b, a, c->stream));
             n += e > b ? 1 : 0;
+        }
+    } else if (c->mode == BTC_MODE_STAGED) {
+        if (c->nslots > 0) {
+            btc::StagedArgs s{};
+            s.tiles = c->tiles;
+            s.slot_tile0 = c->slot_tile0;
+            s.slot_ntiles = c->slot_ntiles;
+            s.slot_coe = c->slot_coe;
+            s.nslots = c->nslots;
+            s.ent = c->tent;
+            s.csr = c->tcsr;
+            s.segs = c->tsegs;
+            s.rows = c->trows;
+            s.val64 = c->tval64;
+            s.A = c->F[0];
+            s.B = c->F[1];
+            s.C = c->F[2];
+            s.R = c->R;
+            s.Rp = c->Rp;
+            s.reg = c->cfg.reg;
+            s.cap = c->st_cap;
+            s.wave = c->st_wave;
+            s.counter = c->counter;
+            CK(cudaMemsetAsync(c->counter, 0, sizeof(int), c->stream));
+            CK(btc::launch_staged(c->dtype, s, c->st_grid, c->st_block, c->stream));
+            n = 1;
         }
     } else {
         return BTC_ERR_UNSUPPORTED;

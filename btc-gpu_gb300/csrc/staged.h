@@ -1,0 +1,38 @@
+// Staged SGD kernel (staged.cu): one CTA per scheduled slot, the slot's rows
+// gathered into shared memory, each row written back once per tile.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "tiles.h"
+
+namespace btc {
+
+struct StagedArgs {
+    const TileHdr* tiles;
+    const int* slot_tile0;   // first tile of each slot's block
+    const int* slot_ntiles;
+    const void* slot_coe;    // 3 per slot, compute type, times lr
+    int nslots;
+    const int4* ent;
+    const unsigned short* csr;
+    const int4* segs;
+    const int* rows;
+    const double* val64;     // FP64 values (f64), else null
+    void* A;
+    void* B;
+    void* C;
+    int R, Rp;
+    double reg;
+    int cap;                 // rows per tile
+    int wave;                // entries per tile
+    int* counter;            // next slot to take (zeroed before each launch)
+};
+
+// Shared-memory bytes of one CTA for a dtype, rank stride, cap and wave.
+size_t staged_smem_bytes(int dtype, int Rp, int cap, int wave);
+// Largest cap that fits `ctas_per_sm` CTAs on one SM.
+int staged_cap_for(int dtype, int Rp, int wave, int ctas_per_sm, size_t smem_per_sm, size_t smem_per_block);
+cudaError_t launch_staged(int dtype, const StagedArgs& a, int grid, int block, cudaStream_t st);
+int staged_blocks_per_sm(int dtype, int R, int block, size_t smem);
+
+}  // namespace btc

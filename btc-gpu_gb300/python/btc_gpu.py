@@ -34,7 +34,8 @@ class Config(ctypes.Structure):
         ("parallel_sequence_size", ctypes.c_int32), ("requested_gpu_count", ctypes.c_int32),
         ("dtype", ctypes.c_int32), ("mode", ctypes.c_int32), ("device", ctypes.c_int32),
         ("resident_blocks", ctypes.c_int32), ("chunk", ctypes.c_int32),
-        ("host_threads", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7),
+        ("host_threads", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 6),
     ]
 
 
