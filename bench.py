@@ -90,7 +90,7 @@ class Clocks:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -325,12 +325,12 @@ def run_gpu(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
     ap.add_argument("--dtype", default="f32", choices=["f32", "f64", "bf16"])
-    ap.add_argument("--mode", default="hogwild", choices=["hogwild", "deterministic", "staged"])
+    ap.add_argument("--mode", default="staged", choices=["hogwild", "deterministic", "staged"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ctas", type=int, default=0, help="staged kernel CTAs per SM (0 = auto)")
     args = ap.parse_args()

@@ -474,7 +474,7 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
 
     if (c->mode == BTC_MODE_STAGED) {
         c->st_wave = std::max(1, std::min(cfg.thread_size, 4096));
-        int ctas = cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 2;
+        int ctas = cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 4;
         c->st_cap = btc::staged_cap_for(c->dtype, c->Rp, c->st_wave, ctas, prop.sharedMemPerMultiprocessor,
                                         prop.sharedMemPerBlockOptin);
         if (c->st_cap < 3)

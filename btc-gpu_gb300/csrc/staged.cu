@@ -2,16 +2,16 @@
 //
 // Persistent CTAs take scheduled slots in schedule order from a global
 // counter.  For each tile of the slot's block (see tiles.cpp):
-//   1. stage   every distinct row of the tile is copied from L2 into shared
-//              memory (snapshot S) with 16-byte ld.cg loads spread over the
-//              whole CTA, and a delta buffer D is cleared;
+//   1. stage   every distinct row of the tile, its entries and CSR lists are
+//              copied from L2 into shared memory (snapshot S) with 16-byte
+//              cp.async copies spread over the whole CTA, all in flight at once;
 //   2. errors  one lane group per entry: dot of the three staged rows,
 //              shuffle-reduced, err = value - dot;
 //   3. owners  one lane group per owner segment (a run of <= seg entries
 //              sharing a row of one mode) sums err * (other two rows) from S
-//              and adds coe*lr*(sum - count*reg*row) into D once;
-//   4. write   every staged row's delta goes back to global memory with one
-//              vector atomic add per 16 bytes.
+//              in registers and adds coe*lr*(sum - count*reg*row) to the row
+//              in global memory with one vector atomic per 16 bytes, so a row
+//              is written once per segment instead of once per entry.
 // Inside a tile the update is the reference kernel's: all entries of one
 // thread_size wave read rows before their deltas land (sgd_Kernel.cu:358-392),
 // coe-weighted, L2-regularised per visit.  Tiles of one slot run in order on
@@ -41,8 +41,6 @@ struct SV<double> {
     using V = double2;
 };
 
-__device__ __forceinline__ float4 zero_v(float) { return make_float4(0.f, 0.f, 0.f, 0.f); }
-__device__ __forceinline__ double2 zero_v(double) { return make_double2(0.0, 0.0); }
 __device__ __forceinline__ void red_v(float* p, float4 d) { atomicAdd(reinterpret_cast<float4*>(p), d); }
 __device__ __forceinline__ void red_v(double* p, double2 d)
 {
@@ -63,6 +61,13 @@ __device__ __forceinline__ double tile_value<double>(const int4&, const double* 
     return __ldg(val64 + idx);
 }
 
+__device__ __forceinline__ void cp16(void* smem_dst, const void* gsrc)
+{
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 template <typename T, int G, int NV>
 __global__ void __launch_bounds__(256) k_staged(StagedArgs a)
 {
@@ -72,11 +77,12 @@ __global__ void __launch_bounds__(256) k_staged(StagedArgs a)
     constexpr int E = NV * VN;
     extern __shared__ __align__(16) unsigned char smem[];
     const int Rp = a.Rp;
+    const StagedLayout L(sizeof(T), Rp, a.cap, a.wave);
     T* S = reinterpret_cast<T*>(smem);
-    T* D = S + (size_t)a.cap * Rp;
-    int4* ent = reinterpret_cast<int4*>(D + (size_t)a.cap * Rp);
-    T* err = reinterpret_cast<T*>(ent + a.wave);
-    unsigned short* csr = reinterpret_cast<unsigned short*>(err + a.wave);
+    int4* ent = reinterpret_cast<int4*>(smem + L.ent);
+    T* err = reinterpret_cast<T*>(smem + L.err);
+    int* rid = reinterpret_cast<int*>(smem + L.rid);
+    unsigned short* csr = reinterpret_cast<unsigned short*>(smem + L.csr);
     __shared__ int s_slot;
 
     const int tid = threadIdx.x;
@@ -104,19 +110,21 @@ __global__ void __launch_bounds__(256) k_staged(StagedArgs a)
             const TileHdr h = a.tiles[t];
             const int nv = h.nrows * vpr;
             const int nxy = h.nx + h.ny;
-            // 1. stage rows and clear deltas
+            // 1. stage: rows, entries and CSR lists, all as 16-byte async copies
             for (int i = tid; i < nv; i += blockDim.x) {
                 const int r = i / vpr, c = i - r * vpr;
                 const int g = __ldg(&a.rows[h.roff + r]);
+                if (c == 0)
+                    rid[r] = g;
                 const T* Fm = r < h.nx ? FA : (r < nxy ? FB : FC);
-                V v = __ldcg(reinterpret_cast<const V*>(Fm + (size_t)g * Rp) + c);
-                reinterpret_cast<V*>(S)[i] = v;
-                reinterpret_cast<V*>(D)[i] = zero_v(T(0));
+                cp16(reinterpret_cast<V*>(S) + i, reinterpret_cast<const V*>(Fm + (size_t)g * Rp) + c);
             }
             for (int i = tid; i < h.n; i += blockDim.x)
-                ent[i] = __ldcs(&a.ent[h.eoff + i]);
-            for (int i = tid; i < 3 * h.n; i += blockDim.x)
-                csr[i] = __ldcs(&a.csr[3 * h.eoff + i]);
+                cp16(ent + i, a.ent + h.eoff + i);
+            const int nc = (3 * h.n + 7) >> 3;
+            for (int i = tid; i < nc; i += blockDim.x)
+                cp16(csr + 8 * i, a.csr + h.coff + 8 * i);
+            cp_wait_all();
             __syncthreads();
             // 2. errors
             for (int e0 = warp * EPW; e0 < h.n; e0 += nwarps * EPW) {
@@ -150,7 +158,7 @@ __global__ void __launch_bounds__(256) k_staged(StagedArgs a)
                     err[e] = tile_value<T>(q, a.val64, h.eoff + e) - p;
             }
             __syncthreads();
-            // 3. owner segments
+            // 3. owner segments: reduce in registers, one vector add per 16 bytes
             for (int s0 = warp * EPW; s0 < h.nseg; s0 += nwarps * EPW) {
                 const int s = s0 + sub;
                 if (s >= h.nseg)
@@ -184,25 +192,21 @@ __global__ void __launch_bounds__(256) k_staged(StagedArgs a)
                     }
                 }
                 const T* sr = S + (size_t)row * Rp;
-                T* dr = D + (size_t)row * Rp;
                 const T w = m == 0 ? cx : (m == 1 ? cy : cz);
                 const T creg = (T)cnt * reg;
+                T* gr = (m == 0 ? FA : (m == 1 ? FB : FC)) + (size_t)rid[row] * Rp;
 #pragma unroll
                 for (int j = 0; j < NV; j++) {
                     const int o = (j * G + gl) * VN;
+                    V d;
+                    T* dd = reinterpret_cast<T*>(&d);
 #pragma unroll
                     for (int i = 0; i < VN; i++)
-                        atomicAdd(dr + o + i, w * (acc[j * VN + i] - creg * sr[o + i]));
+                        dd[i] = w * (acc[j * VN + i] - creg * sr[o + i]);
+                    red_v(gr + o, d);
                 }
             }
-            __syncthreads();
-            // 4. write back each staged row once
-            for (int i = tid; i < nv; i += blockDim.x) {
-                const int r = i / vpr, c = i - r * vpr;
-                const int g = __ldg(&a.rows[h.roff + r]);
-                T* Fm = r < h.nx ? FA : (r < nxy ? FB : FC);
-                red_v(Fm + (size_t)g * Rp + c * VN, reinterpret_cast<const V*>(D)[i]);
-            }
+            // the slot's next tile must see these adds
             __threadfence();
             __syncthreads();
         }
@@ -238,19 +242,17 @@ const void* kernel_for(int R)
 
 size_t staged_smem_bytes(int dtype, int Rp, int cap, int wave)
 {
-    size_t es = dtype == 1 ? 8 : 4;
-    size_t b = 2 * (size_t)cap * Rp * es + (size_t)wave * 16 + (size_t)wave * es + 3 * (size_t)wave * 2;
-    return (b + 15) & ~(size_t)15;
+    return StagedLayout(dtype == 1 ? 8 : 4, Rp, cap, wave).total;
 }
 
 int staged_cap_for(int dtype, int Rp, int wave, int ctas_per_sm, size_t smem_per_sm, size_t smem_per_block)
 {
     size_t es = dtype == 1 ? 8 : 4;
     size_t budget = std::min(smem_per_block, smem_per_sm / (size_t)std::max(1, ctas_per_sm) - 1024);
-    size_t fixed = (size_t)wave * (16 + es + 6) + 64;
-    if (budget <= fixed)
-        return 0;
-    return (int)std::min<size_t>(65535, (budget - fixed) / (2 * (size_t)Rp * es));
+    int cap = (int)std::min<size_t>(65535, budget / ((size_t)Rp * es + 4));
+    while (cap > 0 && staged_smem_bytes(dtype, Rp, cap, wave) > budget)
+        cap--;
+    return cap;
 }
 
 cudaError_t launch_staged(int dtype, const StagedArgs& a, int grid, int block, cudaStream_t st)

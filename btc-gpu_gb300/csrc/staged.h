@@ -28,6 +28,21 @@ struct StagedArgs {
     int* counter;            // next slot to take (zeroed before each launch)
 };
 
+// Shared-memory layout of one CTA: S rows | entries | errors | row ids | CSR.
+// Every region that receives 16-byte copies starts on a 16-byte boundary.
+struct StagedLayout {
+    size_t ent, err, rid, csr, total;
+    __host__ __device__ StagedLayout(size_t es, int Rp, int cap, int wave)
+    {
+        auto al = [](size_t v) { return (v + 15) & ~(size_t)15; };
+        ent = al((size_t)cap * Rp * es);
+        err = al(ent + (size_t)wave * 16);
+        rid = al(err + (size_t)wave * es);
+        csr = al(rid + (size_t)cap * 4);
+        total = al(csr + (3 * (size_t)wave + 8) * 2);
+    }
+};
+
 // Shared-memory bytes of one CTA for a dtype, rank stride, cap and wave.
 size_t staged_smem_bytes(int dtype, int Rp, int cap, int wave);
 // Largest cap that fits `ctas_per_sm` CTAs on one SM.

@@ -44,6 +44,7 @@ void build_tiles(const Schedule& s, const int32_t* xyz, const double* val, int I
         h.roff = (long long)out.rows.size();
         h.eoff = (long long)out.ent.size();
         h.soff = (long long)out.segs.size();
+        h.coff = (long long)out.csr.size();
         h.n = (int)cur.size();
         h.nrows = nx + ny + nz;
         h.nx = nx;
@@ -84,6 +85,8 @@ void build_tiles(const Schedule& s, const int32_t* xyz, const double* val, int I
                 }
             }
         }
+        while (out.csr.size() % 8)
+            out.csr.push_back(0);
         h.nseg = (int)((long long)out.segs.size() - h.soff);
         out.max_rows = std::max(out.max_rows, h.nrows);
         out.max_n = std::max(out.max_n, h.n);

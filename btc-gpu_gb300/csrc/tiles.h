@@ -17,18 +17,19 @@ struct TileHdr {
     long long eoff;
     long long roff;
     long long soff;
+    long long coff;  // csr offset (uint16 units, multiple of 8 so 16-byte copies stay aligned)
     int n;
     int nseg;
     int nrows;
     int nx;
     int ny;
-    int pad;
+    int pad[3];
 };
 
 struct TileSet {
     std::vector<TileHdr> tiles;
     std::vector<int4> ent;        // (lx | ly << 16, lz, 0, value bits): local row ids, y/z offset
-    std::vector<uint16_t> csr;    // per tile 3 x n: entries of each mode ordered by row
+    std::vector<uint16_t> csr;    // per tile 3 x n (padded to 8): entries of each mode ordered by row
     std::vector<int4> segs;       // (local row, mode, start in that mode's csr, count)
     std::vector<int32_t> rows;    // global row id of every staged row
     std::vector<double> val64;    // FP64 entry values (f64 tiles)
