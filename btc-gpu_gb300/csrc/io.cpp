@@ -97,6 +97,8 @@ bool parse_double(const char*& p, const char* end, double& out)
     }
     buf[n] = 0;
     out = std::strtod(buf, nullptr);
+    if (std::isinf(out))
+        return false;  // overflow fails extraction; underflow is accepted
     p = q;
     return true;
 }

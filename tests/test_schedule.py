@@ -1,0 +1,140 @@
+"""Host logic of the product library (no GPU): schedule builder, report,
+shuffle, text reader and the C ABI's exported symbols.
+
+The builder is compared with the golden fixtures produced by the reference's
+own block.cu (tests/golden/make_golden.py): same blocks, groups, coe weights
+and per-slot entry order, and a byte-identical block_parallel.txt.
+"""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import btc_gpu as bg
+import goldens
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CASES = goldens.cases()
+
+
+def _cfg(c, **kw):
+    return bg.config(I=c.meta["I"], J=c.meta["J"], K=c.meta["K"], block_s=c.meta["block_s"],
+                     parallel_sequence_size=c.meta["parallel_sequence_size"], resident_blocks=-1, **kw)
+
+
+@pytest.fixture(scope="module", params=CASES)
+def built(request):
+    c = goldens.Case(request.param)
+    xyz, val = bg.shuffle(c.input_xyz.copy(), c.input_val.copy())
+    return c, xyz, val, bg.Schedule(_cfg(c), xyz)
+
+
+def test_shuffle_matches_reference(built):
+    c, xyz, val, s = built
+    assert np.array_equal(xyz, c.shuffled)
+
+
+def test_blocks_match_reference(built):
+    c, xyz, val, s = built
+    meta, codes = s.blocks()
+    assert c.header["num_block_total"] == s.summary.num_blocks
+    nonempty = [b for b in range(s.summary.num_blocks) if meta[b, 0] > 0]
+    assert [rb["id"] for rb in c.blocks] == nonempty
+    for b, rb in zip(nonempty, c.blocks):
+        assert rb["nnz"] == int(meta[b, 0])
+        assert rb["levels"] == tuple(int(v) for v in meta[b, 1:])
+        for a in range(3):
+            L = int(meta[b, 1 + a])
+            bits = "0" + (format(int(codes[b, a]), "0%db" % (L - 1)) if L > 1 else "")
+            assert rb["ids"][a] == bits
+
+
+def test_groups_slots_coe_match_reference(built):
+    c, xyz, val, s = built
+    off, ids, coe = s.groups()
+    assert [ids[off[i]:off[i + 1]].tolist() for i in range(len(off) - 1)] == [q["ids"] for q in c.seqs]
+    assert s.summary.max_parallel == c.schedule["max_parallel"]
+    assert s.summary.num_groups + 1 == c.schedule["num_parallel"]
+    for k, sl in enumerate(c.schedule["slots"]):
+        assert tuple(float(v) for v in coe[k]) == sl["coe"]
+        ent = s.block_entries(int(ids[k]))
+        assert [tuple(v) for v in xyz[ent].tolist()] == sl["xyz"]
+
+
+def test_report_byte_identical(built, tmp_path):
+    c, xyz, val, s = built
+    p = tmp_path / "block_parallel.txt"
+    s.write_report(str(p))
+    with open(os.path.join(c.dir, "block_parallel.txt"), "rb") as f:
+        assert p.read_bytes() == f.read()
+
+
+def test_reader_skips_like_the_reference(tmp_path):
+    p = tmp_path / "t.train"
+    p.write_text("# comment\n% also\n\n1 2 3 0.5\n4 5 6 7e-1 extra fields\n1.5 2 3 4\nbad line\n"
+                 "  7 8 9   -2.25\n1 2\n3 3 3 inf\n2 2 2 1e\n2 2 2 1e999\n5 5 5 1e-999\n")
+    xyz, val = bg.read_entries(str(p), 1, 10, 10, 10)
+    # the same lines libstdc++'s stream extraction accepts (main.cpp:47-63)
+    assert xyz.tolist() == [[0, 1, 2], [3, 4, 5], [6, 7, 8], [4, 4, 4]]
+    assert val.tolist() == [0.5, 0.7, -2.25, 0.0]
+
+
+def test_reader_rejects_out_of_range(tmp_path):
+    p = tmp_path / "t.train"
+    p.write_text("1 1 1 1.0\n0 1 1 2.0\n")
+    with pytest.raises(bg.BtcError) as e:
+        bg.read_entries(str(p), 1, 5, 5, 5)
+    assert e.value.status == 8 and e.value.line == 2
+
+
+def test_builder_rejects_out_of_range_coordinates():
+    cfg = bg.config(I=4, J=4, K=4, resident_blocks=-1)
+    with pytest.raises(bg.BtcError):
+        bg.Schedule(cfg, np.array([[0, 0, 4]], np.int32))
+
+
+def test_config_validation():
+    assert bg.validate(bg.config()) == 0
+    for kw in (dict(rank=0), dict(rank=129), dict(lr=0.0), dict(reg=-1.0), dict(block_s=0),
+               dict(thread_size=1025), dict(parallel_sequence_size=-1), dict(epochs=0), dict(dtype=7)):
+        assert bg.validate(bg.config(**kw)) != 0, kw
+
+
+def test_abi_exports_every_declared_symbol():
+    with open(os.path.join(ROOT, "include", "btc_gpu.h")) as f:
+        hdr = f.read()
+    declared = set(re.findall(r"\b(btc_[a-z0-9_]+)\s*\(", hdr))
+    declared -= {"btc_status"}
+    lib = bg.lib()
+    missing = [n for n in sorted(declared) if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(bg.SIGNATURES) == declared
+
+
+def test_generator_is_deterministic_and_deduplicated():
+    a = bg.gen_tensor(500, 400, 300, 20000, zipf=(1.2, 1.2, 1.2), gt_rank=4, seed=3)
+    b = bg.gen_tensor(500, 400, 300, 20000, zipf=(1.2, 1.2, 1.2), gt_rank=4, seed=3)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    allx = np.concatenate([a[0], a[2]])
+    assert len(allx) == 20000
+    assert len(np.unique(allx, axis=0)) == 20000
+    assert 0.85 < len(a[1]) / 20000 < 0.95
+
+
+def test_cli_arguments_like_the_reference():
+    cli = bg.CLI_PATH
+    r = subprocess.run([cli, "--help"], capture_output=True, text=True)
+    assert r.returncode == 0 and "Usage:" in r.stderr
+    r = subprocess.run([cli, "ds", "1", "2"], capture_output=True, text=True)
+    assert r.returncode == 1
+    r = subprocess.run([cli, "ds", "10", "10", "10", "/tmp", "0", "/tmp", "--rank", "101"],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and "rank r must be in [1, 100]" in r.stderr
+    r = subprocess.run([cli, "ds", "10", "10", "10", "--bogus=1"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Unknown option: --bogus" in r.stderr
+    r = subprocess.run([cli, "ds", "10", "10", "10", "/tmp", "2"], capture_output=True, text=True)
+    assert r.returncode == 1 and "coord_base must be 0 or 1." in r.stderr
