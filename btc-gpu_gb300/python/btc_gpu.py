@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(PKG, "lib", "libbtcgpu.so")
 CLI_PATH = os.path.join(PKG, "bin", "tensor_sgd")
 
 F32, F64, BF16 = 0, 1, 2
+NOALLOC_MAX_ENTRIES = 67108864
 HOGWILD, DETERMINISTIC, STAGED = 0, 1, 2
 TRAIN, TEST = 0, 1
 
@@ -99,6 +100,7 @@ SIGNATURES = {
     "btc_eval": ([P, I32, P], ctypes.c_int),
     "btc_host_alloc": ([P, I64], ctypes.c_int),
     "btc_device_count": ([P], ctypes.c_int),
+    "btc_eval_sums_noalloc": ([P, P, I64, P, P, P, I32, I32, I64, P, P], ctypes.c_int),
     "btc_device_info": ([I32, ctypes.c_char_p, P, P], ctypes.c_int),
     "btc_host_free": ([P], None),
     "btc_ctx_stream": ([P], P),

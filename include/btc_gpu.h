@@ -201,6 +201,28 @@ btc_status btc_train_epoch_host(btc_ctx *ctx, double *A, double *B, double *C,
 btc_status btc_device_count(int32_t *count);
 btc_status btc_device_info(int32_t device, char *name, int32_t *sm_count, int64_t *memory_bytes);
 
+/* ---- error sums without allocation ----------------------------------------
+ * No counterpart in the reference: an added entry point for callers that
+ * cannot call cudaMalloc -- code running during CUDA graph capture, hosts
+ * whose framework owns every device allocation, allocation-free real-time
+ * loops.  It computes the FP64 sums (SSE, SAE, sum ref^2) of
+ * compute_metrics_gpu over n entries and writes them to sums[0..2].
+ * Every pointer is DEVICE memory supplied by the caller: xyz is n x 3 int32,
+ * val n doubles, A/B/C row-major factors of `dtype` (F32 or F64) with
+ * `row_stride` elements per row (>= rank), sums 3 doubles.  The launch goes
+ * on `stream` (a cudaStream_t, NULL for the default stream) and is not
+ * waited for.
+ * Its only scratch is a file-scope device array of BTC_NOALLOC_MAX_ENTRIES /
+ * 1024 partial triples (1.5 MiB per GPU, held until exit); n above
+ * BTC_NOALLOC_MAX_ENTRIES returns BTC_ERR_RANGE without launching.  The
+ * first call on a device looks up that array's address (call it once before
+ * any stream capture).  All calls on a device share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller. */
+#define BTC_NOALLOC_MAX_ENTRIES 67108864LL
+btc_status btc_eval_sums_noalloc(const int32_t *xyz, const double *val, int64_t n, const void *A,
+                                 const void *B, const void *C, int32_t dtype, int32_t rank,
+                                 int64_t row_stride, double *sums, void *stream);
+
 /* Page-locked host memory for the end-to-end transfers (cudaHostAlloc). */
 btc_status btc_host_alloc(void **p, int64_t bytes);
 void btc_host_free(void *p);
