@@ -17,6 +17,7 @@
 //                              the init is drawn from std::random_device like
 //                              the reference (tensor_SGD.cu:43-53)
 //   --init-lo X --init-hi X    init range (default 0.02, 0.1 as the reference)
+//   --init-file FILE           initial factors as raw doubles A[I*r], B[J*r], C[K*r]
 //   --dump-factors DIR         write A.txt, B.txt, C.txt (rows of %.17g)
 //   --device N                 CUDA device ordinal
 #include <sys/stat.h>
@@ -47,7 +48,7 @@ namespace {
 btc_config cfg;
 string dataset_name = "tensor";
 string output_root = "output";
-string precision = "f32", mode_name = "hogwild", dump_dir;
+string precision = "f32", mode_name = "hogwild", dump_dir, init_file;
 bool have_seed = false;
 unsigned long long seed = 0;
 double init_lo = 0.02, init_hi = 0.1;
@@ -89,6 +90,7 @@ void print_usage(const char* program)
     cerr << "  --mode hogwild|deterministic|staged   Kernel schedule. Default: hogwild" << endl;
     cerr << "  --seed N                      Seeded factor init (default: random_device)" << endl;
     cerr << "  --init-lo X, --init-hi X      Factor init range. Default: 0.02 0.1" << endl;
+    cerr << "  --init-file FILE              Initial factors (raw doubles A, B, C)" << endl;
     cerr << "  --dump-factors DIR            Write the final factors as text" << endl;
     cerr << "  --device N                    CUDA device. Default: 0" << endl;
 }
@@ -142,6 +144,8 @@ bool apply_option(const string& o, const string& v)
         init_hi = atof(v.c_str());
     else if (o == "--dump-factors")
         dump_dir = v;
+    else if (o == "--init-file")
+        init_file = v;
     else if (o == "--device")
         cfg.device = atoi(v.c_str());
     else {
@@ -400,6 +404,19 @@ int main(int argc, char** argv)
             F[m].resize((size_t)rows[m] * r);
             for (auto& v : F[m])
                 v = dist(gen);
+        }
+    }
+    if (!init_file.empty()) {
+        FILE* f = fopen(init_file.c_str(), "rb");
+        size_t got = 0;
+        for (int m = 0; m < 3 && f; m++)
+            got += fread(F[m].data(), sizeof(double), F[m].size(), f);
+        if (f)
+            fclose(f);
+        if (got != (size_t)(cfg.I + (int64_t)cfg.J + cfg.K) * r) {
+            cerr << "Failed to read " << (int64_t)(cfg.I + (int64_t)cfg.J + cfg.K) * r << " initial values from "
+                 << init_file << endl;
+            return 1;
         }
     }
 

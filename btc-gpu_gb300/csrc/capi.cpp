@@ -71,6 +71,13 @@ struct btc_ctx {
     int* trows = nullptr;
     double* tval64 = nullptr;
     int* counter = nullptr;
+    // BF16 storage: FP32 masters of the hottest rows
+    float* master[3] = {nullptr, nullptr, nullptr};
+    int* hot_map[3] = {nullptr, nullptr, nullptr};
+    int* hot_rows[3] = {nullptr, nullptr, nullptr};
+    int nhot[3] = {0, 0, 0};
+    unsigned epoch = 0;
+    int* status = nullptr;
     int st_cap = 0, st_wave = 0, st_grid = 0, st_block = 256;
     long long st_rows = 0, st_tiles = 0;
     int64_t updates = 0;
@@ -334,6 +341,12 @@ btc_status btc_ctx_destroy(btc_ctx* c)
     free_dev(c->trows);
     free_dev(c->tval64);
     free_dev(c->counter);
+    free_dev(c->status);
+    for (int a = 0; a < 3; a++) {
+        free_dev(c->master[a]);
+        free_dev(c->hot_map[a]);
+        free_dev(c->hot_rows[a]);
+    }
     if (c->ev0)
         cudaEventDestroy(c->ev0);
     if (c->ev1)
@@ -365,9 +378,9 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
     CK(cudaEventCreate(&c->ev1));
     c->dtype = cfg.dtype;
     c->mode = cfg.mode;
-    if (c->dtype == BTC_DTYPE_BF16)
-        return BTC_ERR_UNSUPPORTED;
-    c->esize = c->dtype == BTC_DTYPE_F64 ? 8 : 4;
+    if (c->dtype == BTC_DTYPE_BF16 && c->mode != BTC_MODE_STAGED)
+        return BTC_ERR_UNSUPPORTED;  // BF16 storage is served by the staged kernel
+    c->esize = c->dtype == BTC_DTYPE_F64 ? 8 : (c->dtype == BTC_DTYPE_BF16 ? 2 : 4);
     c->R = cfg.rank;
     c->Rp = btc::padded_rank(c->dtype, c->R);
     c->chunk = cfg.chunk > 0 ? cfg.chunk : 128;
@@ -468,6 +481,48 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
         CK(cudaMemsetAsync(c->F[a], 0, bytes, c->stream));
     }
     CK(cudaMalloc((void**)&c->staging, (size_t)maxrows * c->R * sizeof(double)));
+    CK(cudaMalloc((void**)&c->status, sizeof(int)));
+    CK(cudaMemsetAsync(c->status, 0, sizeof(int), c->stream));
+
+    if (c->dtype == BTC_DTYPE_BF16) {
+        // hot rows: updated by many entries per epoch, so their small updates
+        // accumulate in an FP32 master instead of being rounded to BF16 each
+        // time; a row is hot when its update count is at least 8x the mean of
+        // the updated rows (at most 16384 per mode)
+        for (int a = 0; a < 3; a++) {
+            std::vector<int64_t> cnt((size_t)c->rows[a], 0);
+            for (int k = 0; k < nslots; k++)
+                for (int32_t e : s.blocks[(size_t)s.slot_block[k]].ent)
+                    cnt[(size_t)txyz[3 * (int64_t)e + a]]++;
+            int64_t used = 0, total = 0;
+            for (int64_t v : cnt)
+                if (v > 0) {
+                    used++;
+                    total += v;
+                }
+            const double thr = std::max(64.0, used > 0 ? 8.0 * (double)total / (double)used : 0.0);
+            std::vector<int> hot;
+            for (int64_t r = 0; r < c->rows[a]; r++)
+                if ((double)cnt[(size_t)r] >= thr)
+                    hot.push_back((int)r);
+            std::sort(hot.begin(), hot.end(), [&](int x, int y) { return cnt[(size_t)x] > cnt[(size_t)y]; });
+            if (hot.size() > 16384)
+                hot.resize(16384);
+            std::sort(hot.begin(), hot.end());
+            std::vector<int> map((size_t)c->rows[a], -1);
+            for (size_t h = 0; h < hot.size(); h++)
+                map[(size_t)hot[h]] = (int)h;
+            c->nhot[a] = (int)hot.size();
+            if ((rc = upload((void**)&c->hot_map[a], map.data(), map.size() * 4, c->stream)))
+                return rc;
+            if ((rc = upload((void**)&c->hot_rows[a], hot.data(), hot.size() * 4, c->stream)))
+                return rc;
+            CK(cudaMalloc((void**)&c->master[a], std::max<size_t>(16, hot.size() * c->Rp * sizeof(float))));
+            CK(cudaMemsetAsync(c->master[a], 0, std::max<size_t>(16, hot.size() * c->Rp * sizeof(float)),
+                               c->stream));
+        }
+        CK(cudaStreamSynchronize(c->stream));
+    }
 
     int occ = btc::hogwild_blocks_per_sm(c->dtype, c->R, c->hw_block);
     c->hw_grid = c->sms * std::max(1, occ);
@@ -597,6 +652,9 @@ btc_status btc_ctx_set_factors(btc_ctx* c, int32_t mode, const double* host)
     size_t bytes = (size_t)c->rows[mode] * c->R * sizeof(double);
     CK(cudaMemcpyAsync(c->staging, host, bytes, cudaMemcpyHostToDevice, c->stream));
     CK(btc::launch_pack(c->dtype, c->staging, c->F[mode], c->rows[mode], c->R, c->Rp, c->stream));
+    if (c->dtype == BTC_DTYPE_BF16)
+        CK(btc::launch_master(0, c->staging, nullptr, c->master[mode], nullptr, c->hot_rows[mode], c->nhot[mode],
+                              c->R, c->Rp, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return BTC_OK;
 }
@@ -608,6 +666,9 @@ btc_status btc_ctx_get_factors(btc_ctx* c, int32_t mode, double* host)
     CK(cudaSetDevice(c->cfg.device));
     size_t bytes = (size_t)c->rows[mode] * c->R * sizeof(double);
     CK(btc::launch_unpack(c->dtype, c->F[mode], c->staging, c->rows[mode], c->R, c->Rp, c->stream));
+    if (c->dtype == BTC_DTYPE_BF16)
+        CK(btc::launch_master(1, nullptr, c->staging, c->master[mode], nullptr, c->hot_rows[mode], c->nhot[mode],
+                              c->R, c->Rp, c->stream));
     CK(cudaMemcpyAsync(host, c->staging, bytes, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return BTC_OK;
@@ -684,15 +745,41 @@ static btc_status enqueue_epoch(btc_ctx* c, int* launches)
             s.cap = c->st_cap;
             s.wave = c->st_wave;
             s.counter = c->counter;
+            s.status = c->status;
+            for (int a = 0; a < 3; a++) {
+                s.master[a] = c->master[a];
+                s.hot[a] = c->hot_map[a];
+            }
+            c->epoch++;
+            s.seed = (c->epoch * 0x9E3779B9u) ^ 0x5BD1E995u;
             CK(cudaMemsetAsync(c->counter, 0, sizeof(int), c->stream));
             CK(btc::launch_staged(c->dtype, s, c->st_grid, c->st_block, c->stream));
             n = 1;
+            if (c->dtype == BTC_DTYPE_BF16)
+                for (int a = 0; a < 3; a++) {
+                    CK(btc::launch_master(2, nullptr, nullptr, c->master[a], c->F[a], c->hot_rows[a], c->nhot[a],
+                                          c->R, c->Rp, c->stream));
+                    n += c->nhot[a] > 0 ? 1 : 0;
+                }
         }
     } else {
         return BTC_ERR_UNSUPPORTED;
     }
     if (launches)
         *launches = n;
+    return BTC_OK;
+}
+
+static btc_status check_status(btc_ctx* c, int* word)
+{
+    int h = 0;
+    CK(cudaMemcpy(&h, c->status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (word)
+        *word = h;
+    if (h != 0) {
+        CK(cudaMemset(c->status, 0, sizeof(int)));
+        return BTC_ERR_DEVICE;
+    }
     return BTC_OK;
 }
 
@@ -710,13 +797,15 @@ btc_status btc_train_epoch(btc_ctx* c, btc_epoch_stats* st)
     CK(cudaEventSynchronize(c->ev1));
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    int word = 0;
+    btc_status rs = check_status(c, &word);
     if (st) {
         st->kernel_ms = ms;
         st->updates = c->updates;
         st->launches = launches;
-        st->device_status = 0;
+        st->device_status = word;
     }
-    return BTC_OK;
+    return rs;
 }
 
 btc_status btc_train_epochs(btc_ctx* c, int32_t n, btc_epoch_stats* st)
@@ -736,13 +825,15 @@ btc_status btc_train_epochs(btc_ctx* c, int32_t n, btc_epoch_stats* st)
     CK(cudaEventSynchronize(c->ev1));
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    int word = 0;
+    btc_status rs = check_status(c, &word);
     if (st) {
         st->kernel_ms = ms;
         st->updates = c->updates * (int64_t)n;
         st->launches = total;
-        st->device_status = 0;
+        st->device_status = word;
     }
-    return BTC_OK;
+    return rs;
 }
 
 btc_status btc_device_count(int32_t* count)

@@ -18,6 +18,7 @@
 //                 FP64 instance equals the serial FP64 rule bit for bit.
 //  k_metrics   -- compute_metrics_gpu (sgd_Kernel.cu:64-120) with FP64 sums,
 //                 per-CTA partials and a fixed-order final sum.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -67,6 +68,14 @@ __device__ __forceinline__ void ldrow_ro(const double* p, double* r)
     double2 v = __ldg(reinterpret_cast<const double2*>(p));
     r[0] = v.x;
     r[1] = v.y;
+}
+__device__ __forceinline__ void ldrow_ro(const unsigned short* p, float* r)
+{
+    uint2 v = __ldg(reinterpret_cast<const uint2*>(p));
+    r[0] = __uint_as_float(v.x << 16);
+    r[1] = __uint_as_float(v.x & 0xffff0000u);
+    r[2] = __uint_as_float(v.y << 16);
+    r[3] = __uint_as_float(v.y & 0xffff0000u);
 }
 __device__ __forceinline__ void addrow(float* p, const float* d)
 {
@@ -234,10 +243,10 @@ __global__ void __launch_bounds__(128) k_det(const int* wave_slots, int n, SgdAr
     }
 }
 
-template <typename T, int G, int NV>
+template <typename T, int G, int NV, typename ST = T>
 __global__ void __launch_bounds__(kMetricThreads) k_metrics(const int4* coo, const double* val,
-                                                           long long n, const T* A, const T* B,
-                                                           const T* C, int Rp, double* partials)
+                                                           long long n, const ST* A, const ST* B,
+                                                           const ST* C, int Rp, double* partials)
 {
     constexpr int VN = VT<T>::N;
     constexpr int EPW = 32 / G;
@@ -363,16 +372,16 @@ int hogwild_occ(int R, int block)
     return 1;
 }
 
-template <typename T>
-cudaError_t metrics_t(const int4* coo, const double* val, long long n, const T* A, const T* B,
-                      const T* C, int R, int Rp, double* partials, int grid, double* result,
+template <typename T, typename ST = T>
+cudaError_t metrics_t(const int4* coo, const double* val, long long n, const ST* A, const ST* B,
+                      const ST* C, int R, int Rp, double* partials, int grid, double* result,
                       cudaStream_t st)
 {
     int G, NV;
     pick_shape<T>(R, G, NV);
 #define BTC_MT(g, nv)                                                                              \
     if (G == g && NV == nv) {                                                                      \
-        k_metrics<T, g, nv><<<grid, kMetricThreads, 0, st>>>(coo, val, n, A, B, C, Rp, partials); \
+        k_metrics<T, g, nv, ST><<<grid, kMetricThreads, 0, st>>>(coo, val, n, A, B, C, Rp, partials); \
         cudaError_t e = cudaGetLastError();                                                        \
         if (e != cudaSuccess)                                                                      \
             return e;                                                                              \
@@ -409,7 +418,82 @@ __global__ void k_unpack(const T* src, double* dst, long long rows, int R, int R
     }
 }
 
+__global__ void k_pack_bf16(const double* src, unsigned short* dst, long long rows, int R, int Rp)
+{
+    long long n = rows * Rp;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        long long r = i / Rp;
+        int c = (int)(i - r * Rp);
+        dst[i] = c < R ? __bfloat16_as_ushort(__float2bfloat16_rn((float)src[r * R + c])) : (unsigned short)0;
+    }
+}
+
+__global__ void k_unpack_bf16(const unsigned short* src, double* dst, long long rows, int R, int Rp)
+{
+    long long n = rows * R;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        long long r = i / R;
+        int c = (int)(i - r * R);
+        dst[i] = (double)__uint_as_float((unsigned)src[r * Rp + c] << 16);
+    }
+}
+
+// FP32 master rows of the hot rows: hot_rows[h] is the row of master slot h
+__global__ void k_master_pack(const double* src, float* master, const int* hot_rows, int nhot, int R, int Rp)
+{
+    long long n = (long long)nhot * Rp;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        int h = (int)(i / Rp), c = (int)(i - (long long)h * Rp);
+        master[i] = c < R ? (float)src[(long long)hot_rows[h] * R + c] : 0.f;
+    }
+}
+
+__global__ void k_master_unpack(const float* master, double* dst, const int* hot_rows, int nhot, int R, int Rp)
+{
+    long long n = (long long)nhot * R;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        int h = (int)(i / R), c = (int)(i - (long long)h * R);
+        dst[(long long)hot_rows[h] * R + c] = (double)master[(long long)h * Rp + c];
+    }
+}
+
+// BF16 copy of every hot row from its master (round to nearest), so readers of
+// the BF16 factors (metrics, export) see the masters' values.
+__global__ void k_master_refresh(const float* master, unsigned short* dst, const int* hot_rows, int nhot, int Rp)
+{
+    long long n = (long long)nhot * Rp;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        int h = (int)(i / Rp), c = (int)(i - (long long)h * Rp);
+        dst[(long long)hot_rows[h] * Rp + c] = __bfloat16_as_ushort(__float2bfloat16_rn(master[i]));
+    }
+}
+
+int grid_for(long long n)
+{
+    return (int)std::min<long long>(4096, (n + 255) / 256 + 1);
+}
+
 }  // namespace
+
+cudaError_t launch_master(int op, const double* src, double* dst, float* master, void* bf16, const int* hot_rows,
+                          int nhot, int R, int Rp, cudaStream_t st)
+{
+    if (nhot <= 0)
+        return cudaSuccess;
+    const int grid = grid_for((long long)nhot * Rp);
+    if (op == 0)
+        k_master_pack<<<grid, 256, 0, st>>>(src, master, hot_rows, nhot, R, Rp);
+    else if (op == 1)
+        k_master_unpack<<<grid, 256, 0, st>>>(master, dst, hot_rows, nhot, R, Rp);
+    else
+        k_master_refresh<<<grid, 256, 0, st>>>(master, (unsigned short*)bf16, hot_rows, nhot, Rp);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_pack(int dtype, const double* src, void* dst, long long rows, int R, int Rp,
                         cudaStream_t st)
@@ -419,6 +503,8 @@ cudaError_t launch_pack(int dtype, const double* src, void* dst, long long rows,
         k_pack<double><<<grid, 256, 0, st>>>(src, (double*)dst, rows, R, Rp);
     else if (dtype == 0)
         k_pack<float><<<grid, 256, 0, st>>>(src, (float*)dst, rows, R, Rp);
+    else if (dtype == 2)
+        k_pack_bf16<<<grid, 256, 0, st>>>(src, (unsigned short*)dst, rows, R, Rp);
     else
         return cudaErrorInvalidValue;
     return cudaGetLastError();
@@ -432,6 +518,8 @@ cudaError_t launch_unpack(int dtype, const void* src, double* dst, long long row
         k_unpack<double><<<grid, 256, 0, st>>>((const double*)src, dst, rows, R, Rp);
     else if (dtype == 0)
         k_unpack<float><<<grid, 256, 0, st>>>((const float*)src, dst, rows, R, Rp);
+    else if (dtype == 2)
+        k_unpack_bf16<<<grid, 256, 0, st>>>((const unsigned short*)src, dst, rows, R, Rp);
     else
         return cudaErrorInvalidValue;
     return cudaGetLastError();
@@ -445,6 +533,8 @@ int padded_rank(int dtype, int R)
         return G * NV * 2;
     }
     pick_shape<float>(R, G, NV);
+    if (dtype == 2)
+        return (G * NV * 4 + 7) / 8 * 8;  // whole 16-byte BF16 chunks
     return G * NV * 4;
 }
 
@@ -492,6 +582,10 @@ cudaError_t launch_metrics(int dtype, const int4* coo, const double* val, long l
     if (dtype == 0)
         return metrics_t<float>(coo, val, n, (const float*)A, (const float*)B, (const float*)C, R, Rp,
                                 partials, grid, result, st);
+    if (dtype == 2)
+        return metrics_t<float, unsigned short>(coo, val, n, (const unsigned short*)A,
+                                                (const unsigned short*)B, (const unsigned short*)C, R, Rp,
+                                                partials, grid, result, st);
     return cudaErrorInvalidValue;
 }
 

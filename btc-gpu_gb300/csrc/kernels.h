@@ -43,6 +43,11 @@ cudaError_t launch_metrics(int dtype, const int4* coo, const double* val, long l
                            const void* A, const void* B, const void* C, int R, int Rp,
                            double* partials, int grid, double* result, cudaStream_t st);
 constexpr int kMetricThreads = 256;
+// FP32 master rows of a BF16 context: op 0 packs host doubles (src, [rows][R])
+// into the masters, op 1 unpacks the masters over dst ([rows][R]), op 2
+// refreshes the BF16 copy of every hot row from its master.
+cudaError_t launch_master(int op, const double* src, double* dst, float* master, void* bf16, const int* hot_rows,
+                          int nhot, int R, int Rp, cudaStream_t st);
 // double [rows][R] <-> padded device rows [rows][Rp] of the dtype
 cudaError_t launch_pack(int dtype, const double* src, void* dst, long long rows, int R, int Rp,
                         cudaStream_t st);

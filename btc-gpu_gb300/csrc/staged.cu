@@ -61,6 +61,50 @@ __device__ __forceinline__ double tile_value<double>(const int4&, const double* 
     return __ldg(val64 + idx);
 }
 
+// BF16 helpers.  Stochastic rounding follows the published recipe of adding
+// uniform random bits below the truncation point and truncating (Gupta et
+// al., "Deep Learning with Limited Numerical Precision", 2015): the rounded
+// value is unbiased, so updates far below one BF16 ulp still move a row on
+// average.
+__device__ __forceinline__ unsigned mix3(unsigned a, unsigned b, unsigned c)
+{
+    unsigned h = a * 0x9E3779B1u ^ b * 0x85EBCA77u ^ c * 0xC2B2AE3Du;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    h *= 0x297A2D39u;
+    h ^= h >> 15;
+    return h;
+}
+__device__ __forceinline__ unsigned sr_bf16_bits(float x, unsigned r16)
+{
+    unsigned u = __float_as_uint(x);
+    if ((u & 0x7f800000u) == 0x7f800000u)
+        return u >> 16;
+    return (u + (r16 & 0xffffu)) >> 16;
+}
+__device__ __forceinline__ float4 bf16x4_to_float4(uint2 raw)
+{
+    return make_float4(__uint_as_float(raw.x << 16), __uint_as_float(raw.x & 0xffff0000u),
+                       __uint_as_float(raw.y << 16), __uint_as_float(raw.y & 0xffff0000u));
+}
+// Adds (d0, d1) to one BF16 pair with stochastic rounding, by compare-and-
+// swap; gives up (returns false) after a bounded number of attempts.
+__device__ __forceinline__ bool add_pair_sr(unsigned* w, float d0, float d1, unsigned rnd)
+{
+    unsigned old = __ldcg(w);
+    for (int it = 0; it < 1024; it++) {
+        const float lo = __uint_as_float(old << 16) + d0;
+        const float hi = __uint_as_float(old & 0xffff0000u) + d1;
+        const unsigned nw = sr_bf16_bits(lo, rnd) | (sr_bf16_bits(hi, rnd >> 16) << 16);
+        const unsigned prev = atomicCAS(w, old, nw);
+        if (prev == old)
+            return true;
+        old = prev;
+    }
+    return false;
+}
+
 __device__ __forceinline__ void cp16(void* smem_dst, const void* gsrc)
 {
     unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
@@ -68,7 +112,7 @@ __device__ __forceinline__ void cp16(void* smem_dst, const void* gsrc)
 }
 __device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-template <typename T, int G, int NV>
+template <typename T, int G, int NV, bool BF>
 __global__ void __launch_bounds__(256) k_staged(StagedArgs a)
 {
     using V = typename SV<T>::V;
@@ -111,13 +155,33 @@ __global__ void __launch_bounds__(256) k_staged(StagedArgs a)
             const int nv = h.nrows * vpr;
             const int nxy = h.nx + h.ny;
             // 1. stage: rows, entries and CSR lists, all as 16-byte async copies
+            //    (BF16 rows are widened to FP32 through registers)
             for (int i = tid; i < nv; i += blockDim.x) {
                 const int r = i / vpr, c = i - r * vpr;
                 const int g = __ldg(&a.rows[h.roff + r]);
-                if (c == 0)
-                    rid[r] = g;
-                const T* Fm = r < h.nx ? FA : (r < nxy ? FB : FC);
-                cp16(reinterpret_cast<V*>(S) + i, reinterpret_cast<const V*>(Fm + (size_t)g * Rp) + c);
+                if constexpr (BF) {
+                    const int m = r < h.nx ? 0 : (r < nxy ? 1 : 2);
+                    const int* hotm = m == 0 ? a.hot[0] : (m == 1 ? a.hot[1] : a.hot[2]);
+                    const int hm = __ldg(&hotm[g]);
+                    if (c == 0) {
+                        rid[r] = g;
+                        rid[a.cap + r] = hm;
+                    }
+                    if (hm >= 0) {
+                        const float* mm = m == 0 ? a.master[0] : (m == 1 ? a.master[1] : a.master[2]);
+                        cp16(reinterpret_cast<V*>(S) + i, mm + (size_t)hm * Rp + c * 4);
+                    } else {
+                        const unsigned short* Fm = static_cast<const unsigned short*>(
+                            m == 0 ? a.A : (m == 1 ? a.B : a.C));
+                        const uint2 raw = __ldcg(reinterpret_cast<const uint2*>(Fm + (size_t)g * Rp + c * 4));
+                        reinterpret_cast<float4*>(S)[i] = bf16x4_to_float4(raw);
+                    }
+                } else {
+                    if (c == 0)
+                        rid[r] = g;
+                    const T* Fm = r < h.nx ? FA : (r < nxy ? FB : FC);
+                    cp16(reinterpret_cast<V*>(S) + i, reinterpret_cast<const V*>(Fm + (size_t)g * Rp) + c);
+                }
             }
             for (int i = tid; i < h.n; i += blockDim.x)
                 cp16(ent + i, a.ent + h.eoff + i);
@@ -194,16 +258,45 @@ __global__ void __launch_bounds__(256) k_staged(StagedArgs a)
                 const T* sr = S + (size_t)row * Rp;
                 const T w = m == 0 ? cx : (m == 1 ? cy : cz);
                 const T creg = (T)cnt * reg;
-                T* gr = (m == 0 ? FA : (m == 1 ? FB : FC)) + (size_t)rid[row] * Rp;
+                if constexpr (BF) {
+                    const int g = rid[row], hm = rid[a.cap + row];
+                    unsigned short* Fm = static_cast<unsigned short*>(m == 0 ? a.A : (m == 1 ? a.B : a.C));
 #pragma unroll
-                for (int j = 0; j < NV; j++) {
-                    const int o = (j * G + gl) * VN;
-                    V d;
-                    T* dd = reinterpret_cast<T*>(&d);
+                    for (int j = 0; j < NV; j++) {
+                        const int o = (j * G + gl) * VN;
+                        float4 d;
+                        d.x = w * (acc[j * VN + 0] - creg * sr[o + 0]);
+                        d.y = w * (acc[j * VN + 1] - creg * sr[o + 1]);
+                        d.z = w * (acc[j * VN + 2] - creg * sr[o + 2]);
+                        d.w = w * (acc[j * VN + 3] - creg * sr[o + 3]);
+                        if (hm >= 0) {
+                            float* mm = m == 0 ? a.master[0] : (m == 1 ? a.master[1] : a.master[2]);
+                            red_v(mm + (size_t)hm * Rp + o, d);
+                        } else {
+                            unsigned* wp = reinterpret_cast<unsigned*>(Fm + (size_t)g * Rp + o);
+                            const unsigned rnd0 = mix3(a.seed ^ (unsigned)(m * 0x68E31DA4u), (unsigned)g, (unsigned)o);
+                            const unsigned rnd1 = mix3(a.seed ^ (unsigned)(m * 0x68E31DA4u), (unsigned)g, (unsigned)o + 2);
+                            bool ok = true;
+                            if (d.x != 0.f || d.y != 0.f)
+                                ok &= add_pair_sr(wp, d.x, d.y, rnd0);
+                            if (d.z != 0.f || d.w != 0.f)
+                                ok &= add_pair_sr(wp + 1, d.z, d.w, rnd1);
+                            if (!ok)
+                                atomicExch(a.status, 1);
+                        }
+                    }
+                } else {
+                    T* gr = (m == 0 ? FA : (m == 1 ? FB : FC)) + (size_t)rid[row] * Rp;
 #pragma unroll
-                    for (int i = 0; i < VN; i++)
-                        dd[i] = w * (acc[j * VN + i] - creg * sr[o + i]);
-                    red_v(gr + o, d);
+                    for (int j = 0; j < NV; j++) {
+                        const int o = (j * G + gl) * VN;
+                        V d;
+                        T* dd = reinterpret_cast<T*>(&d);
+#pragma unroll
+                        for (int i = 0; i < VN; i++)
+                            dd[i] = w * (acc[j * VN + i] - creg * sr[o + i]);
+                        red_v(gr + o, d);
+                    }
                 }
             }
             // the slot's next tile must see these adds
@@ -225,17 +318,26 @@ void pick(int R, int& G, int& NV)
         NV++;
 }
 
-template <typename T>
+template <typename T, bool BF>
 const void* kernel_for(int R)
 {
     int G, NV;
     pick<T>(R, G, NV);
 #define BTC_KS(g, nv)                                 \
     if (G == g && NV == nv)                           \
-        return (const void*)&k_staged<T, g, nv>;
+        return (const void*)&k_staged<T, g, nv, BF>;
     BTC_KS(1, 1) BTC_KS(2, 1) BTC_KS(4, 1) BTC_KS(8, 1) BTC_KS(16, 1) BTC_KS(32, 1) BTC_KS(32, 2)
 #undef BTC_KS
     return nullptr;
+}
+
+const void* kernel_for_dtype(int dtype, int R)
+{
+    if (dtype == 1)
+        return kernel_for<double, false>(R);
+    if (dtype == 2)
+        return kernel_for<float, true>(R);
+    return kernel_for<float, false>(R);
 }
 
 }  // namespace
@@ -257,7 +359,7 @@ int staged_cap_for(int dtype, int Rp, int wave, int ctas_per_sm, size_t smem_per
 
 cudaError_t launch_staged(int dtype, const StagedArgs& a, int grid, int block, cudaStream_t st)
 {
-    const void* fn = dtype == 1 ? kernel_for<double>(a.R) : kernel_for<float>(a.R);
+    const void* fn = kernel_for_dtype(dtype, a.R);
     if (!fn)
         return cudaErrorInvalidValue;
     size_t smem = staged_smem_bytes(dtype, a.Rp, a.cap, a.wave);
@@ -270,7 +372,7 @@ cudaError_t launch_staged(int dtype, const StagedArgs& a, int grid, int block, c
 
 int staged_blocks_per_sm(int dtype, int R, int block, size_t smem)
 {
-    const void* fn = dtype == 1 ? kernel_for<double>(R) : kernel_for<float>(R);
+    const void* fn = kernel_for_dtype(dtype, R);
     if (!fn)
         return 0;
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)

@@ -26,9 +26,15 @@ struct StagedArgs {
     int cap;                 // rows per tile
     int wave;                // entries per tile
     int* counter;            // next slot to take (zeroed before each launch)
+    // BF16 storage only
+    float* master[3];        // FP32 master rows of the hottest rows of each mode
+    const int* hot[3];       // row -> master index, -1 when the row has none
+    unsigned seed;           // stochastic-rounding stream of this epoch
+    int* status;             // set to 1 when a rounding compare-and-swap gives up
 };
 
-// Shared-memory layout of one CTA: S rows | entries | errors | row ids | CSR.
+// Shared-memory layout of one CTA: S rows | entries | errors | row ids and
+// master slots | CSR.
 // Every region that receives 16-byte copies starts on a 16-byte boundary.
 struct StagedLayout {
     size_t ent, err, rid, csr, total;
@@ -38,7 +44,7 @@ struct StagedLayout {
         ent = al((size_t)cap * Rp * es);
         err = al(ent + (size_t)wave * 16);
         rid = al(err + (size_t)wave * es);
-        csr = al(rid + (size_t)cap * 4);
+        csr = al(rid + (size_t)cap * 8);
         total = al(csr + (3 * (size_t)wave + 8) * 2);
     }
 };

@@ -130,3 +130,46 @@ def test_factor_roundtrip_and_init():
         ctx.init_factors(99, 0.0, 0.1)
         assert np.array_equal(a1, ctx.get_factors(0))
         assert a1.min() >= 0.0 and a1.max() < 0.1 and abs(a1.mean() - 0.05) < 0.005
+
+
+@pytest.mark.parametrize("case_name,R", [("cube1000_20k", 16), ("zipf13_6k", 32), ("bigdim", 100)])
+def test_bf16_staged_close_to_fp32(case_name, R):
+    """BF16 storage (FP32 math, stochastic rounding, FP32 masters of the
+    hottest rows) stays within 1% of the FP32 run's test RMSE."""
+    c, xyz, val, init, sched = _setup(case_name, R)
+    ctx32 = _ctx(c, xyz, val, R, bg.F32, bg.STAGED)
+    ctx16 = _ctx(c, xyz, val, R, bg.BF16, bg.STAGED)
+    for m in range(3):
+        ctx32.set_factors(m, init[m])
+        ctx16.set_factors(m, init[m])
+    for epoch in range(5):
+        st = ctx16.train_epoch()
+        assert st.device_status == 0
+        ctx32.train_epoch()
+        r16, r32 = ctx16.eval(bg.TEST).rmse, ctx32.eval(bg.TEST).rmse
+        assert abs(r16 - r32) / r32 <= 1e-2, (epoch, r16, r32)
+
+
+def test_bf16_stochastic_rounding_is_unbiased():
+    """Updates far below one BF16 ulp still move the rows on average: the mean
+    BF16 change matches the FP32 change (round-to-nearest would lose it)."""
+    R = 16
+    c, xyz, val, init, sched = _setup("cube1000_20k", R)
+    I, J, K = c.dims
+    cfg = dict(I=I, J=J, K=K, rank=R, lr=2e-3, reg=0.0, block_s=c.meta["block_s"],
+               parallel_sequence_size=c.meta["parallel_sequence_size"], mode=bg.STAGED, resident_blocks=-1)
+    s = bg.Schedule(bg.config(**cfg), xyz)
+    base = [np.full((n, R), 0.0625) for n in (I, J, K)]  # exactly representable in BF16
+    out = {}
+    for dt in (bg.F32, bg.BF16):
+        ctx = bg.Context(bg.config(dtype=dt, **cfg), s, xyz, val, xyz, val)
+        for m in range(3):
+            ctx.set_factors(m, base[m])
+        ctx.train_epoch()
+        out[dt] = [ctx.get_factors(m) - base[m] for m in range(3)]
+        ctx.close()
+    d32 = np.concatenate([d.ravel() for d in out[bg.F32]])
+    d16 = np.concatenate([d.ravel() for d in out[bg.BF16]])
+    ulp = 0.0625 * 2.0 ** -7
+    assert np.abs(d32).mean() < 0.5 * ulp  # typical updates are below one ulp ...
+    assert abs(d16.mean() - d32.mean()) <= 0.05 * np.abs(d32).mean()  # ... and survive on average
