@@ -159,6 +159,7 @@ def test_bf16_stochastic_rounding_is_unbiased():
     cfg = dict(I=I, J=J, K=K, rank=R, lr=2e-3, reg=0.0, block_s=c.meta["block_s"],
                parallel_sequence_size=c.meta["parallel_sequence_size"], mode=bg.STAGED, resident_blocks=-1)
     s = bg.Schedule(bg.config(**cfg), xyz)
+    val = np.ones(len(val))  # every update pushes the same way, about 0.3 ulp per row in total
     base = [np.full((n, R), 0.0625) for n in (I, J, K)]  # exactly representable in BF16
     out = {}
     for dt in (bg.F32, bg.BF16):
@@ -171,5 +172,5 @@ def test_bf16_stochastic_rounding_is_unbiased():
     d32 = np.concatenate([d.ravel() for d in out[bg.F32]])
     d16 = np.concatenate([d.ravel() for d in out[bg.BF16]])
     ulp = 0.0625 * 2.0 ** -7
-    assert np.abs(d32).mean() < 0.5 * ulp  # typical updates are below one ulp ...
-    assert abs(d16.mean() - d32.mean()) <= 0.05 * np.abs(d32).mean()  # ... and survive on average
+    assert 0 < d32.mean() < 0.5 * ulp  # the whole epoch moves a row by less than one ulp ...
+    assert abs(d16.mean() - d32.mean()) <= 0.05 * d32.mean()  # ... and the BF16 rows move as much on average
