@@ -484,45 +484,6 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
     CK(cudaMalloc((void**)&c->status, sizeof(int)));
     CK(cudaMemsetAsync(c->status, 0, sizeof(int), c->stream));
 
-    if (c->dtype == BTC_DTYPE_BF16) {
-        // hot rows: updated by many entries per epoch, so their small updates
-        // accumulate in an FP32 master instead of being rounded to BF16 each
-        // time; a row is hot when its update count is at least 8x the mean of
-        // the updated rows (at most 16384 per mode)
-        for (int a = 0; a < 3; a++) {
-            std::vector<int64_t> cnt((size_t)c->rows[a], 0);
-            for (int k = 0; k < nslots; k++)
-                for (int32_t e : s.blocks[(size_t)s.slot_block[k]].ent)
-                    cnt[(size_t)txyz[3 * (int64_t)e + a]]++;
-            int64_t used = 0, total = 0;
-            for (int64_t v : cnt)
-                if (v > 0) {
-                    used++;
-                    total += v;
-                }
-            const double thr = std::max(64.0, used > 0 ? 8.0 * (double)total / (double)used : 0.0);
-            std::vector<int> hot;
-            for (int64_t r = 0; r < c->rows[a]; r++)
-                if ((double)cnt[(size_t)r] >= thr)
-                    hot.push_back((int)r);
-            std::sort(hot.begin(), hot.end(), [&](int x, int y) { return cnt[(size_t)x] > cnt[(size_t)y]; });
-            if (hot.size() > 16384)
-                hot.resize(16384);
-            std::sort(hot.begin(), hot.end());
-            std::vector<int> map((size_t)c->rows[a], -1);
-            for (size_t h = 0; h < hot.size(); h++)
-                map[(size_t)hot[h]] = (int)h;
-            c->nhot[a] = (int)hot.size();
-            if ((rc = upload((void**)&c->hot_map[a], map.data(), map.size() * 4, c->stream)))
-                return rc;
-            if ((rc = upload((void**)&c->hot_rows[a], hot.data(), hot.size() * 4, c->stream)))
-                return rc;
-            CK(cudaMalloc((void**)&c->master[a], std::max<size_t>(16, hot.size() * c->Rp * sizeof(float))));
-            CK(cudaMemsetAsync(c->master[a], 0, std::max<size_t>(16, hot.size() * c->Rp * sizeof(float)),
-                               c->stream));
-        }
-        CK(cudaStreamSynchronize(c->stream));
-    }
 
     int occ = btc::hogwild_blocks_per_sm(c->dtype, c->R, c->hw_block);
     c->hw_grid = c->sms * std::max(1, occ);
@@ -560,6 +521,53 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
             return rc;
         if (!ts.val64.empty() && (rc = upload((void**)&c->tval64, ts.val64.data(), ts.val64.size() * 8, c->stream)))
             return rc;
+        if (c->dtype == BTC_DTYPE_BF16) {
+            // FP32 masters for the rows whose BF16 copy would be contended:
+            // every row that a tile updates through more than one owner
+            // segment (those segments add to it concurrently) and every row
+            // updated at least 4x as often as the mean row; their small
+            // updates then accumulate exactly instead of being rounded to
+            // BF16 each time.  The other rows take at most one stochastically
+            // rounded compare-and-swap per tile.
+            for (int a = 0; a < 3; a++) {
+                std::vector<int64_t> cnt((size_t)c->rows[a], 0);
+                for (int k = 0; k < nslots; k++)
+                    for (int32_t e : s.blocks[(size_t)s.slot_block[k]].ent)
+                        cnt[(size_t)txyz[3 * (int64_t)e + a]]++;
+                int64_t used = 0, total = 0;
+                for (int64_t v : cnt)
+                    if (v > 0) {
+                        used++;
+                        total += v;
+                    }
+                const double thr = used > 0 ? 4.0 * (double)total / (double)used : 0.0;
+                std::vector<char> is_hot((size_t)c->rows[a], 0);
+                for (int64_t r = 0; r < c->rows[a]; r++)
+                    is_hot[(size_t)r] = cnt[(size_t)r] > 0 && (double)cnt[(size_t)r] >= thr;
+                for (const btc::TileHdr& h : ts.tiles)
+                    for (int q = 1; q < h.nseg; q++) {
+                        const int4& s0 = ts.segs[(size_t)(h.soff + q - 1)];
+                        const int4& s1 = ts.segs[(size_t)(h.soff + q)];
+                        if (s1.y == a && s0.y == a && s0.x == s1.x)
+                            is_hot[(size_t)ts.rows[(size_t)(h.roff + s1.x)]] = 1;
+                    }
+                std::vector<int> hot;
+                for (int64_t r = 0; r < c->rows[a]; r++)
+                    if (is_hot[(size_t)r])
+                        hot.push_back((int)r);
+                std::vector<int> map((size_t)c->rows[a], -1);
+                for (size_t h = 0; h < hot.size(); h++)
+                    map[(size_t)hot[h]] = (int)h;
+                c->nhot[a] = (int)hot.size();
+                if ((rc = upload((void**)&c->hot_map[a], map.data(), map.size() * 4, c->stream)))
+                    return rc;
+                if ((rc = upload((void**)&c->hot_rows[a], hot.data(), hot.size() * 4, c->stream)))
+                    return rc;
+                const size_t mb = std::max<size_t>(16, hot.size() * c->Rp * sizeof(float));
+                CK(cudaMalloc((void**)&c->master[a], mb));
+                CK(cudaMemsetAsync(c->master[a], 0, mb, c->stream));
+            }
+        }
         CK(cudaMalloc((void**)&c->counter, sizeof(int)));
         size_t smem = btc::staged_smem_bytes(c->dtype, c->Rp, c->st_cap, c->st_wave);
         int occ = btc::staged_blocks_per_sm(c->dtype, c->R, c->st_block, smem);

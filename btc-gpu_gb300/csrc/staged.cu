@@ -93,7 +93,7 @@ __device__ __forceinline__ float4 bf16x4_to_float4(uint2 raw)
 __device__ __forceinline__ bool add_pair_sr(unsigned* w, float d0, float d1, unsigned rnd)
 {
     unsigned old = __ldcg(w);
-    for (int it = 0; it < 1024; it++) {
+    for (int it = 0; it < (1 << 16); it++) {
         const float lo = __uint_as_float(old << 16) + d0;
         const float hi = __uint_as_float(old & 0xffff0000u) + d1;
         const unsigned nw = sr_bf16_bits(lo, rnd) | (sr_bf16_bits(hi, rnd >> 16) << 16);
