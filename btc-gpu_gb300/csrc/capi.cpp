@@ -71,6 +71,8 @@ struct btc_ctx {
     int* trows = nullptr;
     double* tval64 = nullptr;
     int* counter = nullptr;
+    int* unit_off = nullptr;       // device, nunits + 1
+    int nunits = 0;
     // BF16 storage: FP32 masters of the hottest rows
     float* master[3] = {nullptr, nullptr, nullptr};
     int* hot_map[3] = {nullptr, nullptr, nullptr};
@@ -79,6 +81,10 @@ struct btc_ctx {
     unsigned epoch = 0;
     int* status = nullptr;
     int st_cap = 0, st_wave = 0, st_grid = 0, st_block = 256;
+    std::vector<float> tile_feat;  // BTC_TILE_FEATURES per tile
+    std::vector<int> h_tile0, h_ntiles;  // host copy of each slot's tiles
+    unsigned* tile_ns = nullptr;   // device, allocated on the first profiled epoch
+    bool profile_next = false;
     long long st_rows = 0, st_tiles = 0;
     int64_t updates = 0;
     int nslots = 0;
@@ -341,7 +347,9 @@ btc_status btc_ctx_destroy(btc_ctx* c)
     free_dev(c->trows);
     free_dev(c->tval64);
     free_dev(c->counter);
+    free_dev(c->unit_off);
     free_dev(c->status);
+    free_dev(c->tile_ns);
     for (int a = 0; a < 3; a++) {
         free_dev(c->master[a]);
         free_dev(c->hot_map[a]);
@@ -505,6 +513,30 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
         }
         c->st_tiles = (long long)ts.tiles.size();
         c->st_rows = (long long)ts.rows.size();
+        c->h_tile0 = t0;
+        c->h_ntiles = tn;
+        c->tile_feat.assign(ts.tiles.size() * BTC_TILE_FEATURES, 0.f);
+        for (size_t t = 0; t < ts.tiles.size(); t++) {
+            const btc::TileHdr& h = ts.tiles[t];
+            int maxseg = 0;
+            for (int q = 0; q < h.nseg; q++)
+                maxseg = std::max(maxseg, ts.segs[(size_t)(h.soff + q)].w);
+            float* f = &c->tile_feat[t * BTC_TILE_FEATURES];
+            const float nr = (float)std::max(1, h.nrows);
+            f[0] = (float)h.n / (float)c->st_wave;
+            f[1] = (float)h.nrows / (float)c->st_cap;
+            f[2] = (float)h.nx / nr;
+            f[3] = (float)h.ny / nr;
+            f[4] = (float)h.nseg / (float)std::max(1, h.n);
+            f[5] = (float)maxseg / 16.f;
+            f[6] = std::log2(1.f + (float)h.n) / 10.f;
+            f[7] = std::log2(1.f + (float)h.nrows) / 10.f;
+            f[8] = (float)h.n / nr / 8.f;
+            f[9] = 0.f;
+        }
+        for (size_t b = 0; b < ts.block_tile0.size(); b++)
+            if (ts.block_tile0[b] >= 0)
+                c->tile_feat[(size_t)ts.block_tile0[b] * BTC_TILE_FEATURES + 9] = 1.f;
         if ((rc = upload((void**)&c->tiles, ts.tiles.data(), ts.tiles.size() * sizeof(btc::TileHdr), c->stream)))
             return rc;
         if ((rc = upload((void**)&c->slot_tile0, t0.data(), t0.size() * 4, c->stream)))
@@ -569,6 +601,14 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
             }
         }
         CK(cudaMalloc((void**)&c->counter, sizeof(int)));
+        {
+            std::vector<int> uo((size_t)nslots + 1);
+            for (int k = 0; k <= nslots; k++)
+                uo[(size_t)k] = k;  // one slot per unit until a packing is chosen
+            if ((rc = upload((void**)&c->unit_off, uo.data(), uo.size() * 4, c->stream)))
+                return rc;
+            c->nunits = nslots;
+        }
         size_t smem = btc::staged_smem_bytes(c->dtype, c->Rp, c->st_cap, c->st_wave);
         int occ = btc::staged_blocks_per_sm(c->dtype, c->R, c->st_block, smem);
         if (occ <= 0)
@@ -739,6 +779,8 @@ static btc_status enqueue_epoch(btc_ctx* c, int* launches)
             s.slot_ntiles = c->slot_ntiles;
             s.slot_coe = c->slot_coe;
             s.nslots = c->nslots;
+            s.unit_off = c->unit_off;
+            s.nunits = c->nunits;
             s.ent = c->tent;
             s.csr = c->tcsr;
             s.segs = c->tsegs;
@@ -754,6 +796,7 @@ static btc_status enqueue_epoch(btc_ctx* c, int* launches)
             s.wave = c->st_wave;
             s.counter = c->counter;
             s.status = c->status;
+            s.tile_ns = c->profile_next ? c->tile_ns : nullptr;
             for (int a = 0; a < 3; a++) {
                 s.master[a] = c->master[a];
                 s.hot[a] = c->hot_map[a];
@@ -842,6 +885,170 @@ btc_status btc_train_epochs(btc_ctx* c, int32_t n, btc_epoch_stats* st)
         st->device_status = word;
     }
     return rs;
+}
+
+btc_status btc_ctx_set_work_units(btc_ctx* c, const int32_t* unit_off, int32_t nunits)
+{
+    if (!c || c->mode != BTC_MODE_STAGED || nunits < 0 || (nunits > 0 && !unit_off))
+        return BTC_ERR_ARG;
+    if (nunits == 0 || unit_off[0] != 0 || unit_off[nunits] != c->nslots)
+        return BTC_ERR_ARG;
+    for (int32_t u = 0; u < nunits; u++)
+        if (unit_off[u + 1] <= unit_off[u])
+            return BTC_ERR_ARG;
+    CK(cudaSetDevice(c->cfg.device));
+    free_dev(c->unit_off);
+    btc_status rc = upload((void**)&c->unit_off, unit_off, ((size_t)nunits + 1) * 4, c->stream);
+    if (rc)
+        return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    c->nunits = nunits;
+    return BTC_OK;
+}
+
+btc_status btc_ctx_slot_tiles(btc_ctx* c, int32_t* tile0, int32_t* ntiles)
+{
+    if (!c || !tile0 || !ntiles || c->mode != BTC_MODE_STAGED)
+        return BTC_ERR_ARG;
+    CK(cudaMemcpy(tile0, c->slot_tile0, (size_t)c->nslots * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ntiles, c->slot_ntiles, (size_t)c->nslots * 4, cudaMemcpyDeviceToHost));
+    return BTC_OK;
+}
+
+// The learned work-unit packing of the staged kernel:
+// 1. profile  one training epoch records the time of every tile;
+// 2. learn    the MLP (mlp.cu) is trained on the GPU to map a tile's features
+//             to log(time in microseconds);
+// 3. propose  every tile's time is predicted; a slot's cost is the sum over
+//             its tiles plus the measured per-slot overhead (CTA time spent
+//             outside tiles: taking work from the global counter, slot
+//             set-up); consecutive slots are packed into units of about equal
+//             predicted cost, at least 8 per CTA so that no CTA is left with a
+//             long last unit;
+// 4. judge    epochs with the proposed units and with one slot per unit are
+//             timed alternately; the faster packing stays.
+btc_status btc_ctx_learn_work_units(btc_ctx* c, btc_mlp* model, int32_t train_steps, int32_t judge_epochs,
+                                    btc_learn_report* rep)
+{
+    if (!c || !model || train_steps < 0 || judge_epochs < 1 || !rep || c->mode != BTC_MODE_STAGED)
+        return BTC_ERR_ARG;
+    btc_learn_report r{};
+    const int64_t ntiles = c->st_tiles;
+    if (ntiles == 0 || c->nslots == 0)
+        return BTC_ERR_STATE;
+    std::vector<int> plain((size_t)c->nslots + 1);
+    for (int k = 0; k <= c->nslots; k++)
+        plain[(size_t)k] = k;
+    btc_status rc = btc_ctx_set_work_units(c, plain.data(), c->nslots);
+    if (rc)
+        return rc;
+    std::vector<uint32_t> ns((size_t)ntiles);
+    btc_epoch_stats es{};
+    if ((rc = btc_train_epoch_profiled(c, ns.data(), &es)))
+        return rc;
+    std::vector<float> x, y;
+    double tile_us = 0;
+    for (int64_t t = 0; t < ntiles; t++) {
+        if (ns[(size_t)t] == 0)
+            continue;
+        x.insert(x.end(), c->tile_feat.begin() + t * BTC_TILE_FEATURES,
+                 c->tile_feat.begin() + (t + 1) * BTC_TILE_FEATURES);
+        y.push_back(std::log(std::max(1e-3f, (float)ns[(size_t)t] * 1e-3f)));
+    }
+    // time of each executed tile instance: a block's tiles run once per slot
+    for (int k = 0; k < c->nslots; k++)
+        for (int t = c->h_tile0[(size_t)k]; t < c->h_tile0[(size_t)k] + c->h_ntiles[(size_t)k]; t++)
+            tile_us += ns[(size_t)t] * 1e-3;
+    r.samples = (int64_t)y.size();
+    if (r.samples < 16)
+        return BTC_ERR_STATE;
+    if ((rc = btc_mlp_train(model, x.data(), y.data(), r.samples, train_steps, 3e-3f, &r.model_loss)))
+        return rc;
+    double mean = 0, var = 0;
+    for (float v : y)
+        mean += v;
+    mean /= (double)y.size();
+    for (float v : y)
+        var += (v - mean) * (v - mean);
+    var /= (double)y.size();
+    r.model_r2 = var > 0 ? 1.0 - r.model_loss / var : 0.0;
+    std::vector<float> pred((size_t)ntiles);
+    if ((rc = btc_mlp_predict(model, c->tile_feat.data(), ntiles, pred.data())))
+        return rc;
+    // per-slot overhead: CTA time of the epoch not spent inside tiles
+    const double cta_us = es.kernel_ms * 1e3 * c->st_grid;
+    const double overhead = std::max(0.0, (cta_us - tile_us) / c->nslots);
+    std::vector<double> cost((size_t)c->nslots);
+    double total = 0;
+    for (int k = 0; k < c->nslots; k++) {
+        double v = overhead;
+        for (int t = c->h_tile0[(size_t)k]; t < c->h_tile0[(size_t)k] + c->h_ntiles[(size_t)k]; t++)
+            v += std::exp((double)pred[(size_t)t]);
+        cost[(size_t)k] = v;
+        total += v;
+    }
+    const double target = total / ((double)c->st_grid * 8.0);
+    std::vector<int> units(1, 0);
+    double acc = 0;
+    for (int k = 0; k < c->nslots; k++) {
+        acc += cost[(size_t)k];
+        if (acc >= target || k + 1 == c->nslots) {
+            units.push_back(k + 1);
+            acc = 0;
+        }
+    }
+    r.units = (int32_t)units.size() - 1;
+    // judge: alternate the two packings
+    double t_plain = 0, t_learn = 0;
+    for (int e = 0; e < judge_epochs; e++) {
+        btc_epoch_stats a{}, b{};
+        if ((rc = btc_ctx_set_work_units(c, plain.data(), c->nslots)) || (rc = btc_train_epoch(c, &a)))
+            return rc;
+        if ((rc = btc_ctx_set_work_units(c, units.data(), r.units)) || (rc = btc_train_epoch(c, &b)))
+            return rc;
+        t_plain += a.kernel_ms;
+        t_learn += b.kernel_ms;
+    }
+    r.plain_ms = t_plain / judge_epochs;
+    r.learned_ms = t_learn / judge_epochs;
+    r.kept = r.learned_ms < r.plain_ms ? 1 : 0;
+    if (!r.kept && (rc = btc_ctx_set_work_units(c, plain.data(), c->nslots)))
+        return rc;
+    *rep = r;
+    return BTC_OK;
+}
+
+btc_status btc_ctx_tile_count(btc_ctx* c, int64_t* n)
+{
+    if (!c || !n)
+        return BTC_ERR_ARG;
+    *n = c->mode == BTC_MODE_STAGED ? (int64_t)c->st_tiles : 0;
+    return BTC_OK;
+}
+
+btc_status btc_ctx_tile_features(btc_ctx* c, float* f)
+{
+    if (!c || !f || c->mode != BTC_MODE_STAGED)
+        return BTC_ERR_ARG;
+    std::copy(c->tile_feat.begin(), c->tile_feat.end(), f);
+    return BTC_OK;
+}
+
+btc_status btc_train_epoch_profiled(btc_ctx* c, uint32_t* tile_ns, btc_epoch_stats* st)
+{
+    if (!c || !tile_ns || c->mode != BTC_MODE_STAGED)
+        return BTC_ERR_ARG;
+    CK(cudaSetDevice(c->cfg.device));
+    if (!c->tile_ns)
+        CK(cudaMalloc((void**)&c->tile_ns, std::max<size_t>(16, (size_t)c->st_tiles * sizeof(unsigned))));
+    CK(cudaMemsetAsync(c->tile_ns, 0, std::max<size_t>(16, (size_t)c->st_tiles * sizeof(unsigned)), c->stream));
+    c->profile_next = true;
+    btc_status rc = btc_train_epoch(c, st);
+    c->profile_next = false;
+    if (rc)
+        return rc;
+    CK(cudaMemcpy(tile_ns, c->tile_ns, (size_t)c->st_tiles * sizeof(unsigned), cudaMemcpyDeviceToHost));
+    return BTC_OK;
 }
 
 btc_status btc_device_count(int32_t* count)

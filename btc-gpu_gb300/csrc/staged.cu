@@ -1,7 +1,7 @@
 // k_staged: the shared-memory staged SGD kernel.
 //
-// Persistent CTAs take scheduled slots in schedule order from a global
-// counter.  For each tile of the slot's block (see tiles.cpp):
+// Persistent CTAs take work units (runs of consecutive scheduled slots, in
+// schedule order) from a global counter.  For each tile of the slot's block (see tiles.cpp):
 //   1. stage   every distinct row of the tile, its entries and CSR lists are
 //              copied from L2 into shared memory (snapshot S) with 16-byte
 //              cp.async copies spread over the whole CTA, all in flight at once;
@@ -144,13 +144,18 @@ __global__ void __launch_bounds__(256) k_staged(StagedArgs a)
         if (tid == 0)
             s_slot = atomicAdd(a.counter, 1);
         __syncthreads();
-        const int slot = s_slot;
-        if (slot >= a.nslots)
+        const int unit = s_slot;
+        if (unit >= a.nunits)
             break;
+        const int u0 = __ldg(&a.unit_off[unit]), u1 = __ldg(&a.unit_off[unit + 1]);
+      for (int slot = u0; slot < u1; slot++) {
         const T cx = coe[3 * slot], cy = coe[3 * slot + 1], cz = coe[3 * slot + 2];
         const int t0 = __ldg(&a.slot_tile0[slot]);
         const int t1 = t0 + __ldg(&a.slot_ntiles[slot]);
         for (int t = t0; t < t1; t++) {
+            unsigned long long t_start = 0;
+            if (a.tile_ns && tid == 0)
+                asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
             const TileHdr h = a.tiles[t];
             const int nv = h.nrows * vpr;
             const int nxy = h.nx + h.ny;
@@ -302,7 +307,13 @@ __global__ void __launch_bounds__(256) k_staged(StagedArgs a)
             // the slot's next tile must see these adds
             __threadfence();
             __syncthreads();
+            if (a.tile_ns && tid == 0) {
+                unsigned long long t_end;
+                asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_end));
+                a.tile_ns[t] = (unsigned)min(t_end - t_start, 0xffffffffull);
+            }
         }
+      }
     }
 }
 

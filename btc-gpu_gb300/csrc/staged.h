@@ -13,6 +13,8 @@ struct StagedArgs {
     const int* slot_ntiles;
     const void* slot_coe;    // 3 per slot, compute type, times lr
     int nslots;
+    const int* unit_off;     // work units: slots [unit_off[u], unit_off[u+1]) go to one CTA
+    int nunits;
     const int4* ent;
     const unsigned short* csr;
     const int4* segs;
@@ -31,6 +33,7 @@ struct StagedArgs {
     const int* hot[3];       // row -> master index, -1 when the row has none
     unsigned seed;           // stochastic-rounding stream of this epoch
     int* status;             // set to 1 when a rounding compare-and-swap gives up
+    unsigned* tile_ns;       // when set: nanoseconds each tile took (globaltimer)
 };
 
 // Shared-memory layout of one CTA: S rows | entries | errors | row ids and

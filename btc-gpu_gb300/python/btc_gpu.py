@@ -16,6 +16,7 @@ CLI_PATH = os.path.join(PKG, "bin", "tensor_sgd")
 
 F32, F64, BF16 = 0, 1, 2
 NOALLOC_MAX_ENTRIES = 67108864
+TILE_FEATURES = 10
 HOGWILD, DETERMINISTIC, STAGED = 0, 1, 2
 TRAIN, TEST = 0, 1
 
@@ -100,6 +101,20 @@ SIGNATURES = {
     "btc_eval": ([P, I32, P], ctypes.c_int),
     "btc_host_alloc": ([P, I64], ctypes.c_int),
     "btc_device_count": ([P], ctypes.c_int),
+    "btc_ctx_tile_count": ([P, P], ctypes.c_int),
+    "btc_mlp_create": ([I32, I32, U64, I32, P], ctypes.c_int),
+    "btc_mlp_destroy": ([P], ctypes.c_int),
+    "btc_mlp_param_count": ([P, P], ctypes.c_int),
+    "btc_mlp_get_params": ([P, P], ctypes.c_int),
+    "btc_mlp_set_params": ([P, P], ctypes.c_int),
+    "btc_mlp_gradient": ([P, P, P, I64, P, P], ctypes.c_int),
+    "btc_mlp_train": ([P, P, P, I64, I32, ctypes.c_float, P], ctypes.c_int),
+    "btc_mlp_predict": ([P, P, I64, P], ctypes.c_int),
+    "btc_ctx_learn_work_units": ([P, P, I32, I32, P], ctypes.c_int),
+    "btc_ctx_slot_tiles": ([P, P, P], ctypes.c_int),
+    "btc_ctx_set_work_units": ([P, P, I32], ctypes.c_int),
+    "btc_ctx_tile_features": ([P, P], ctypes.c_int),
+    "btc_train_epoch_profiled": ([P, P, P], ctypes.c_int),
     "btc_eval_sums_noalloc": ([P, P, I64, P, P, P, I32, I32, I64, P, P], ctypes.c_int),
     "btc_device_info": ([I32, ctypes.c_char_p, P, P], ctypes.c_int),
     "btc_host_free": ([P], None),
@@ -204,6 +219,71 @@ def gen_tensor(I, J, K, nnz, zipf=(0.0, 0.0, 0.0), gt_rank=8, gt_std=0.5, noise_
         for p in ptrs:
             L.btc_free(p)
     return tuple(out)
+
+
+class LearnReport(ctypes.Structure):
+    _fields_ = [("plain_ms", ctypes.c_double), ("learned_ms", ctypes.c_double),
+                ("model_loss", ctypes.c_double), ("model_r2", ctypes.c_double),
+                ("samples", ctypes.c_int64), ("units", ctypes.c_int32), ("kept", ctypes.c_int32)]
+
+
+class MLP:
+    """The cost model: n_in -> 32 -> 32 -> 1 (tanh), trained on the GPU."""
+
+    def __init__(self, n_in=None, hidden=32, seed=1, device=0):
+        n_in = TILE_FEATURES if n_in is None else n_in
+        h = ctypes.c_void_p()
+        _ck(_lib().btc_mlp_create(n_in, hidden, seed, device, ctypes.byref(h)), "btc_mlp_create")
+        self._h = h
+        self.n_in = n_in
+        n = ctypes.c_int64()
+        _ck(_lib().btc_mlp_param_count(h, ctypes.byref(n)), "btc_mlp_param_count")
+        self.nparam = n.value
+
+    @property
+    def handle(self):
+        return self._h
+
+    def params(self):
+        p = np.zeros(self.nparam, np.float32)
+        _ck(_lib().btc_mlp_get_params(self._h, _p(p)), "btc_mlp_get_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        _ck(_lib().btc_mlp_set_params(self._h, _p(p)), "btc_mlp_set_params")
+
+    def gradient(self, x, y):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        g = np.zeros(self.nparam, np.float32)
+        loss = ctypes.c_double()
+        _ck(_lib().btc_mlp_gradient(self._h, _p(x), _p(y), len(y), _p(g), ctypes.byref(loss)), "btc_mlp_gradient")
+        return g, loss.value
+
+    def train(self, x, y, steps, lr=3e-3):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        loss = ctypes.c_double()
+        _ck(_lib().btc_mlp_train(self._h, _p(x), _p(y), len(y), steps, lr, ctypes.byref(loss)), "btc_mlp_train")
+        return loss.value
+
+    def predict(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.zeros(len(x), np.float32)
+        _ck(_lib().btc_mlp_predict(self._h, _p(x), len(x), _p(y)), "btc_mlp_predict")
+        return y
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib().btc_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class PinnedArray:
@@ -333,6 +413,37 @@ class Context:
         st = EpochStats()
         _ck(_lib().btc_train_epochs(self._h, n, ctypes.byref(st)), "btc_train_epochs")
         return st
+
+    def tile_features(self):
+        n = ctypes.c_int64()
+        _ck(_lib().btc_ctx_tile_count(self._h, ctypes.byref(n)), "btc_ctx_tile_count")
+        f = np.zeros((n.value, TILE_FEATURES), np.float32)
+        _ck(_lib().btc_ctx_tile_features(self._h, _p(f)), "btc_ctx_tile_features")
+        return f
+
+    def slot_tiles(self, nslots):
+        t0 = np.zeros(max(nslots, 1), np.int32)
+        tn = np.zeros(max(nslots, 1), np.int32)
+        _ck(_lib().btc_ctx_slot_tiles(self._h, _p(t0), _p(tn)), "btc_ctx_slot_tiles")
+        return t0[:nslots], tn[:nslots]
+
+    def set_work_units(self, unit_off):
+        u = np.ascontiguousarray(unit_off, np.int32)
+        _ck(_lib().btc_ctx_set_work_units(self._h, _p(u), len(u) - 1), "btc_ctx_set_work_units")
+
+    def learn_work_units(self, model, train_steps=300, judge_epochs=3):
+        r = LearnReport()
+        _ck(_lib().btc_ctx_learn_work_units(self._h, model.handle, train_steps, judge_epochs, ctypes.byref(r)),
+            "btc_ctx_learn_work_units")
+        return r
+
+    def train_epoch_profiled(self):
+        n = ctypes.c_int64()
+        _ck(_lib().btc_ctx_tile_count(self._h, ctypes.byref(n)), "btc_ctx_tile_count")
+        ns = np.zeros(max(n.value, 1), np.uint32)
+        st = EpochStats()
+        _ck(_lib().btc_train_epoch_profiled(self._h, _p(ns), ctypes.byref(st)), "btc_train_epoch_profiled")
+        return st, ns[: n.value]
 
     def eval(self, split=TEST):
         m = Metrics()

@@ -186,6 +186,61 @@ btc_status btc_train_epochs(btc_ctx *ctx, int32_t n, btc_epoch_stats *stats);
 /* compute_metrics_gpu (sgd_Kernel.cu:136-201) on the train or test split;
  * FP64 sums on the GPU.  count 0 gives NaN metrics like the reference. */
 btc_status btc_eval(btc_ctx *ctx, int32_t split, btc_metrics *out);
+/* ---- per-tile timing and features (staged contexts) -----------------------
+ * No counterpart in the reference: the data the learned cost model trains
+ * on.  A tile is a run of one scheduled block's entries whose rows fit in
+ * shared memory; BTC_TILE_FEATURES floats describe each (entries, staged rows,
+ * row mix per mode, owner segments, longest segment, reuse, position in its
+ * block).  btc_train_epoch_profiled is a normal training epoch that also
+ * returns the nanoseconds each tile took on the GPU (%globaltimer). */
+#define BTC_TILE_FEATURES 10
+btc_status btc_ctx_tile_count(btc_ctx *ctx, int64_t *n);
+btc_status btc_ctx_tile_features(btc_ctx *ctx, float *features);
+btc_status btc_train_epoch_profiled(btc_ctx *ctx, uint32_t *tile_ns, btc_epoch_stats *stats);
+/* The tiles of each scheduled slot: tile0[slot], ntiles[slot] (num_slots each). */
+btc_status btc_ctx_slot_tiles(btc_ctx *ctx, int32_t *tile0, int32_t *ntiles);
+/* Work units of the staged kernel: a CTA takes slots [unit_off[u],
+ * unit_off[u+1]) at once (schedule order is kept).  unit_off[0] = 0,
+ * unit_off[nunits] = num_slots, strictly increasing.  The default is one slot
+ * per unit. */
+btc_status btc_ctx_set_work_units(btc_ctx *ctx, const int32_t *unit_off, int32_t nunits);
+
+/* ---- learned cost model ---------------------------------------------------
+ * No counterpart in the reference.  A small MLP (n_in -> 32 -> 32 -> 1, tanh)
+ * whose forward, backward and Adam kernels are this library's own CUDA code.
+ * It learns the time of a tile from BTC_TILE_FEATURES features (trained on
+ * log microseconds recorded by btc_train_epoch_profiled) and proposes the
+ * work units of the staged kernel: runs of consecutive slots of balanced
+ * predicted cost, so that CTAs take work less often without straggling.  The
+ * plain heuristic (one slot per unit) is the fallback and measured epoch time
+ * decides. */
+typedef struct btc_mlp btc_mlp;
+btc_status btc_mlp_create(int32_t n_in, int32_t n_hidden, uint64_t seed, int32_t device, btc_mlp **out);
+btc_status btc_mlp_destroy(btc_mlp *m);
+btc_status btc_mlp_param_count(const btc_mlp *m, int64_t *n);
+btc_status btc_mlp_get_params(btc_mlp *m, float *host);
+btc_status btc_mlp_set_params(btc_mlp *m, const float *host);
+/* full-batch mean-squared-error gradient (n samples, n_in features each) */
+btc_status btc_mlp_gradient(btc_mlp *m, const float *x, const float *y, int64_t n, float *grad, double *loss);
+/* `steps` full-batch Adam steps; *final_loss is the loss after the last one */
+btc_status btc_mlp_train(btc_mlp *m, const float *x, const float *y, int64_t n, int32_t steps, float lr,
+                         double *final_loss);
+btc_status btc_mlp_predict(btc_mlp *m, const float *x, int64_t n, float *y);
+
+typedef struct btc_learn_report {
+    double plain_ms;      /* mean measured epoch time, one slot per unit */
+    double learned_ms;    /* mean measured epoch time with the proposed units */
+    double model_loss;    /* training loss (mean squared error of log microseconds) */
+    double model_r2;      /* fraction of tile-time variance the model explains */
+    int64_t samples;      /* tiles the model was trained on */
+    int32_t units;        /* work units proposed */
+    int32_t kept;         /* 1: the proposed units were kept; 0: the heuristic stayed */
+} btc_learn_report;
+/* profile one epoch, train `model`, propose units, time judge_epochs epochs of
+ * each (they are training epochs) and keep the faster */
+btc_status btc_ctx_learn_work_units(btc_ctx *ctx, btc_mlp *model, int32_t train_steps, int32_t judge_epochs,
+                                    btc_learn_report *report);
+
 /* Device stream the context launches on (a cudaStream_t). */
 void *btc_ctx_stream(btc_ctx *ctx);
 btc_status btc_ctx_destroy(btc_ctx *ctx);
