@@ -43,20 +43,23 @@ sys.path.insert(0, os.path.join(ROOT, "btc-gpu_gb300", "python"))
 
 WORKLOADS = {
     "c2": dict(I=100000, J=100000, K=10000, nnz=50_000_000, zipf=(1.2, 1.2, 1.2), gt_rank=16,
-               noise=0.05, train=0.9, R=32, lr=0.005, reg=0.02,
+               noise=0.05, train=0.9, R=32, lr=0.005, reg=0.02, epochs=20,
                desc="skewed medium: I=J=100k K=10k, 50M nnz Zipf(1.2) per mode, rank-16 GT + N(0,0.05), "
                     "90/10 split, R=32, lr 0.005, lambda 0.02"),
     "c1": dict(I=1000, J=1000, K=1000, nnz=1_000_000, zipf=(0.0, 0.0, 0.0), gt_rank=8, noise=0.01,
-               train=0.9, R=16, lr=0.01, reg=0.01,
+               train=0.9, R=16, lr=0.01, reg=0.01, epochs=10,
                desc="plain small: I=J=K=1000, 1M nnz uniform, rank-8 GT + N(0,0.01), 90/10 split, R=16, "
                     "lr 0.01, lambda 0.01"),
     "small": dict(I=20000, J=20000, K=5000, nnz=2_000_000, zipf=(1.2, 1.2, 1.2), gt_rank=16, noise=0.05,
-                  train=0.9, R=32, lr=0.005, reg=0.02,
+                  train=0.9, R=32, lr=0.005, reg=0.02, epochs=10,
                   desc="small skewed: I=J=20k K=5k, 2M nnz Zipf(1.2), R=32"),
 }
 METRIC = "nnz-updates/s & time-to-test-RMSE, tuned vs plain FP32, 1×GB300, % HBM peak"
 SEED = 20261203 + 1
 CTAS = 0
+# DRAM bytes per launch of the timed kernel from an ncu capture of the same
+# workload (profiles/), keyed by (workload, dtype, mode); absent = null
+TRAFFIC = {("c2", "f32", "staged"): 2.117e9, ("c2", "f32", "hogwild"): 0.7786e9}
 
 
 def log(*a):
@@ -208,6 +211,43 @@ def run_reference(args):
     return 0
 
 
+def _timed(ctx, steps, dist):
+    """K back-to-back epochs between barriers; device ms (max over ranks)."""
+    if dist:
+        dist.barrier()
+    st = ctx.train_epochs(steps)
+    ms = st.kernel_ms
+    if dist:
+        import torch
+
+        tt = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    return st, ms
+
+
+def _trajectory(ctx, w, epochs):
+    """Fresh init, then per-epoch (cumulative device ms, test RMSE)."""
+    import btc_gpu as bg
+
+    init = init_factors(w)
+    for m in range(3):
+        ctx.set_factors(m, init[m])
+    t, out = 0.0, []
+    for _ in range(epochs):
+        st = ctx.train_epoch()
+        t += st.kernel_ms
+        out.append((t, ctx.eval(bg.TEST).rmse))
+    return out
+
+
+def _time_to(traj, target):
+    for t, r in traj:
+        if r <= target:
+            return t
+    return None
+
+
 def run_gpu(args):
     import btc_gpu as bg
 
@@ -232,42 +272,45 @@ def run_gpu(args):
     log("workload %s: train %d test %d, gen %.1fs schedule %.1fs; blocks %d strata %d groups %d slots %d "
         "updates/epoch %d" % (args.workload, len(tv), len(sv), tgen, tsched, sm.num_blocks, sm.num_strata,
                               sm.num_groups, sm.num_slots, sm.scheduled_updates))
-    ctx = bg.Context(cfg, sched, tx, tv, sx, sv)
+    upd_per_step = sm.scheduled_updates
     init = init_factors(w)
+
+    # the tuned path: staged kernel, chosen precision, autotuned, learned work units
+    ctx = bg.Context(cfg, sched, tx, tv, sx, sv)
     for m in range(3):
         ctx.set_factors(m, init[m])
     ctx.train_epochs(args.warmup)
+    tune = learn = None
+    if mode == bg.STAGED and not args.no_tune:
+        tune = ctx.autotune(2)
+        model = bg.MLP()
+        learn = ctx.learn_work_units(model, train_steps=300, judge_epochs=2)
+        model.close()
+        log("autotune: G=%d NV=%d ctas/SM=%d (%d candidates) %.3f -> %.3f ms; learned units: %d, R2 %.3f, "
+            "plain %.3f ms learned %.3f ms kept %d" % (tune.lanes_per_entry, tune.vectors_per_lane,
+                                                       tune.ctas_per_sm, tune.candidates, tune.default_ms,
+                                                       tune.best_ms, learn.units, learn.model_r2, learn.plain_ms,
+                                                       learn.learned_ms, learn.kept))
     rm0 = ctx.eval(bg.TEST).rmse
-
     clocks = Clocks(local)
-    if dist:
-        dist.barrier()
     clocks.start()
-    st = ctx.train_epochs(args.steps)
+    st, ms = _timed(ctx, args.steps, dist)
     clk = clocks.stop()
-    ms = st.kernel_ms
-    if dist:
-        import torch
-
-        tt = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    upd_per_step = sm.scheduled_updates
     value = upd_per_step * args.steps * world / (ms / 1000.0)
     rm1 = ctx.eval(bg.TEST).rmse
 
     # end to end through the host-buffer call
     shapes = [(n, w["R"]) for n in (w["I"], w["J"], w["K"])]
-    pinned = [bg.PinnedArray(s) for s in shapes]
-    for p, a in zip(pinned, init):
-        p.array[...] = a
+    pinned = [bg.PinnedArray(s_) for s_ in shapes]
+    for p_, a in zip(pinned, init):
+        p_.array[...] = a
     e2e_steps = max(1, min(args.steps, 5))
-    ctx.train_epoch_host(*(p.array for p in pinned))
+    ctx.train_epoch_host(*(p_.array for p_ in pinned))
     if dist:
         dist.barrier()
     t = time.perf_counter()
     for _ in range(e2e_steps):
-        _, met = ctx.train_epoch_host(*(p.array for p in pinned))
+        _, met = ctx.train_epoch_host(*(p_.array for p_ in pinned))
     e2e_s = time.perf_counter() - t
     if dist:
         import torch
@@ -278,17 +321,43 @@ def run_gpu(args):
     fac_bytes = sum(n * w["R"] * 8 for n in (w["I"], w["J"], w["K"]))
     e2e = {"value": upd_per_step * e2e_steps * world / e2e_s, "unit": "updates/s",
            "h2d_bytes_per_step": fac_bytes, "d2h_bytes_per_step": fac_bytes + 24}
+    traj_tuned = _trajectory(ctx, w, w["epochs"]) if not args.no_plain else None
+    for p_ in pinned:
+        p_.free()
+    ctx.close()
+
+    # the plain FP32 path (the reference kernel's execution model on every SM)
+    # and, for context, the staged FP32 kernel untuned
+    plain = staged32 = None
+    traj_plain = None
+    if not args.no_plain:
+        for name, (dt_, md_) in (("plain", (bg.F32, bg.HOGWILD)), ("staged32", (bg.F32, bg.STAGED))):
+            c2 = bg.Context(cfg_for(w, dt_, md_, device=local), sched, tx, tv, sx, sv)
+            for m in range(3):
+                c2.set_factors(m, init[m])
+            c2.train_epochs(args.warmup)
+            st2, ms2 = _timed(c2, args.steps, dist)
+            res = {"value": upd_per_step * args.steps * world / (ms2 / 1000.0), "ms_per_step": ms2 / args.steps,
+                   "dtype": "f32", "mode": "hogwild" if md_ == bg.HOGWILD else "staged"}
+            if name == "plain":
+                traj_plain = _trajectory(c2, w, w["epochs"])
+                plain = res
+            else:
+                staged32 = res
+            c2.close()
 
     peak, src = peaks()
     s_f = {"f32": 4, "f64": 8, "bf16": 2}[args.dtype]
     s_v = 8 if args.dtype == "f64" else 4
     b_upd = 12 + s_v + 6 * w["R"] * s_f
-    per_launch_ms = ms / max(1, st.launches)
-    upd_per_launch = upd_per_step * args.steps / max(1, st.launches)
-    achieved = b_upd * upd_per_launch / (per_launch_ms / 1000.0) / 1e9
+    per_launch_ms = ms / max(1, args.steps)
+    achieved = b_upd * upd_per_step / (per_launch_ms / 1000.0) / 1e9
+    kern = {bg.HOGWILD: "k_hogwild", bg.STAGED: "k_staged"}.get(mode, "k_det")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "peak_source": src, "bytes_per_update": b_upd,
-                "kernel": {bg.HOGWILD: "k_hogwild", bg.STAGED: "k_staged"}.get(mode, "k_det")}
+                "traffic": TRAFFIC.get((args.workload, args.dtype, args.mode)), "peak_source": src,
+                "bytes_per_update": b_upd, "kernel": kern,
+                "note": "algorithmic bytes (indices, value, three rows read and written per update); factor rows "
+                        "stay in L2, so DRAM traffic (ncu, 'traffic') is far lower"}
 
     line = None
     if rank == 0:
@@ -310,12 +379,26 @@ def run_gpu(args):
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": st.launches,
                 "train_nnz_per_s": len(tv) * args.steps * world / (ms / 1000.0),
                 "test_rmse": {"after_warmup": rm0, "after_timed": rm1, "e2e_last": met.rmse}}
+        if tune is not None:
+            line["autotune"] = {"lanes_per_entry": tune.lanes_per_entry, "vectors_per_lane": tune.vectors_per_lane,
+                                "ctas_per_sm": tune.ctas_per_sm, "candidates": tune.candidates,
+                                "default_ms": tune.default_ms, "best_ms": tune.best_ms}
+            line["learned_work_units"] = {"units": learn.units, "model_r2": learn.model_r2,
+                                          "samples": learn.samples, "plain_ms": learn.plain_ms,
+                                          "learned_ms": learn.learned_ms, "kept": bool(learn.kept)}
+        if plain is not None:
+            line["plain_fp32"] = plain
+            line["staged_fp32_untuned"] = staged32
+            target = traj_plain[-1][1] * 1.01
+            tt, tp = _time_to(traj_tuned, target), _time_to(traj_plain, target)
+            line["time_to_rmse"] = {
+                "target": target, "epochs": w["epochs"], "tuned_ms": tt, "plain_ms": tp,
+                "speedup": (tp / tt) if (tt and tp) else None,
+                "tuned_final_rmse": traj_tuned[-1][1], "plain_final_rmse": traj_plain[-1][1],
+                "tuned_vs_plain_rmse_rel": abs(traj_tuned[-1][1] - traj_plain[-1][1]) / traj_plain[-1][1]}
         if clk:
             line["clocks"] = clk
         print(json.dumps(line), flush=True)
-    for p in pinned:
-        p.free()
-    ctx.close()
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -329,10 +412,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
-    ap.add_argument("--dtype", default="f32", choices=["f32", "f64", "bf16"])
+    ap.add_argument("--dtype", default="bf16", choices=["f32", "f64", "bf16"])
     ap.add_argument("--mode", default="staged", choices=["hogwild", "deterministic", "staged"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ctas", type=int, default=0, help="staged kernel CTAs per SM (0 = auto)")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner and the learned work units")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison")
     args = ap.parse_args()
     global CTAS
     CTAS = args.ctas

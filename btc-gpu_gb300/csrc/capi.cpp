@@ -80,7 +80,8 @@ struct btc_ctx {
     int nhot[3] = {0, 0, 0};
     unsigned epoch = 0;
     int* status = nullptr;
-    int st_cap = 0, st_wave = 0, st_grid = 0, st_block = 256;
+    int st_cap = 0, st_wave = 0, st_grid = 0, st_block = 256, st_G = 0, st_NV = 0;
+    size_t st_smem = 0;
     std::vector<float> tile_feat;  // BTC_TILE_FEATURES per tile
     std::vector<int> h_tile0, h_ntiles;  // host copy of each slot's tiles
     unsigned* tile_ns = nullptr;   // device, allocated on the first profiled epoch
@@ -610,6 +611,7 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
             c->nunits = nslots;
         }
         size_t smem = btc::staged_smem_bytes(c->dtype, c->Rp, c->st_cap, c->st_wave);
+        c->st_smem = smem;
         int occ = btc::staged_blocks_per_sm(c->dtype, c->R, c->st_block, smem);
         if (occ <= 0)
             return BTC_ERR_UNSUPPORTED;
@@ -795,6 +797,8 @@ static btc_status enqueue_epoch(btc_ctx* c, int* launches)
             s.cap = c->st_cap;
             s.wave = c->st_wave;
             s.counter = c->counter;
+            s.G = c->st_G;
+            s.NV = c->st_NV;
             s.status = c->status;
             s.tile_ns = c->profile_next ? c->tile_ns : nullptr;
             for (int a = 0; a < 3; a++) {
@@ -1015,6 +1019,56 @@ btc_status btc_ctx_learn_work_units(btc_ctx* c, btc_mlp* model, int32_t train_st
     if (!r.kept && (rc = btc_ctx_set_work_units(c, plain.data(), c->nslots)))
         return rc;
     *rep = r;
+    return BTC_OK;
+}
+
+btc_status btc_ctx_autotune(btc_ctx* c, int32_t epochs, btc_autotune_report* rep)
+{
+    if (!c || epochs < 1 || !rep || c->mode != BTC_MODE_STAGED)
+        return BTC_ERR_ARG;
+    CK(cudaSetDevice(c->cfg.device));
+    int G0, NV0;
+    btc::staged_default_shape(c->dtype, c->R, &G0, &NV0);
+    std::vector<std::pair<int, int>> shapes;
+    shapes.push_back({G0, NV0});
+    if (G0 >= 2 && btc::staged_shape_exists(c->dtype, c->R, G0 / 2, NV0 * 2))
+        shapes.push_back({G0 / 2, NV0 * 2});
+    if (NV0 >= 2 && NV0 % 2 == 0 && btc::staged_shape_exists(c->dtype, c->R, G0 * 2, NV0 / 2))
+        shapes.push_back({G0 * 2, NV0 / 2});
+    const int def_grid = c->st_grid;
+    double best = 1e300, def_ms = 0;
+    int bG = G0, bNV = NV0, bgrid = def_grid, n = 0;
+    for (auto& sh : shapes) {
+        int occ = btc::staged_blocks_per_sm_shape(c->dtype, c->R, sh.first, sh.second, c->st_block, c->st_smem);
+        for (int k = 2; k <= occ; k++) {
+            c->st_G = sh.first;
+            c->st_NV = sh.second;
+            c->st_grid = c->sms * k;
+            btc_epoch_stats st{};
+            btc_status rc = btc_train_epochs(c, epochs, &st);
+            if (rc)
+                return rc;
+            const double ms = st.kernel_ms / epochs;
+            n++;
+            if (sh.first == G0 && sh.second == NV0 && c->st_grid == def_grid)
+                def_ms = ms;
+            if (ms < best) {
+                best = ms;
+                bG = sh.first;
+                bNV = sh.second;
+                bgrid = c->st_grid;
+            }
+        }
+    }
+    c->st_G = bG;
+    c->st_NV = bNV;
+    c->st_grid = bgrid;
+    rep->lanes_per_entry = bG;
+    rep->vectors_per_lane = bNV;
+    rep->ctas_per_sm = bgrid / std::max(1, c->sms);
+    rep->candidates = n;
+    rep->best_ms = best;
+    rep->default_ms = def_ms;
     return BTC_OK;
 }
 

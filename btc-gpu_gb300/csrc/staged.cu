@@ -16,6 +16,7 @@
 // thread_size wave read rows before their deltas land (sgd_Kernel.cu:358-392),
 // coe-weighted, L2-regularised per visit.  Tiles of one slot run in order on
 // the same CTA; different slots run concurrently and compose additively.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -105,6 +106,16 @@ __device__ __forceinline__ bool add_pair_sr(unsigned* w, float d0, float d1, uns
     return false;
 }
 
+__device__ __forceinline__ float4 ld_bf4(const unsigned short* p)
+{
+    return bf16x4_to_float4(*reinterpret_cast<const uint2*>(p));
+}
+__device__ __forceinline__ unsigned pack_bf16x2_rn(float lo, float hi)
+{
+    return (unsigned)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
+           ((unsigned)__bfloat16_as_ushort(__float2bfloat16_rn(hi)) << 16);
+}
+
 __device__ __forceinline__ void cp16(void* smem_dst, const void* gsrc)
 {
     unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
@@ -113,7 +124,7 @@ __device__ __forceinline__ void cp16(void* smem_dst, const void* gsrc)
 __device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 template <typename T, int G, int NV, bool BF>
-__global__ void __launch_bounds__(256) k_staged(StagedArgs a)
+__global__ void __launch_bounds__(256, 4) k_staged(StagedArgs a)
 {
     using V = typename SV<T>::V;
     constexpr int VN = SV<T>::N;
@@ -121,7 +132,7 @@ __global__ void __launch_bounds__(256) k_staged(StagedArgs a)
     constexpr int E = NV * VN;
     extern __shared__ __align__(16) unsigned char smem[];
     const int Rp = a.Rp;
-    const StagedLayout L(sizeof(T), Rp, a.cap, a.wave);
+    const StagedLayout L(BF ? 2 : sizeof(T), Rp, a.cap, a.wave);
     T* S = reinterpret_cast<T*>(smem);
     int4* ent = reinterpret_cast<int4*>(smem + L.ent);
     T* err = reinterpret_cast<T*>(smem + L.err);
@@ -161,10 +172,13 @@ __global__ void __launch_bounds__(256) k_staged(StagedArgs a)
             const int nxy = h.nx + h.ny;
             // 1. stage: rows, entries and CSR lists, all as 16-byte async copies
             //    (BF16 rows are widened to FP32 through registers)
-            for (int i = tid; i < nv; i += blockDim.x) {
-                const int r = i / vpr, c = i - r * vpr;
-                const int g = __ldg(&a.rows[h.roff + r]);
-                if constexpr (BF) {
+            if constexpr (BF) {
+                const int cpr = Rp / 8;  // 16-byte chunks per BF16 row
+                const int nc = h.nrows * cpr;
+                unsigned short* Sb = reinterpret_cast<unsigned short*>(smem);
+                for (int i = tid; i < nc; i += blockDim.x) {
+                    const int r = i / cpr, c = i - r * cpr;
+                    const int g = __ldg(&a.rows[h.roff + r]);
                     const int m = r < h.nx ? 0 : (r < nxy ? 1 : 2);
                     const int* hotm = m == 0 ? a.hot[0] : (m == 1 ? a.hot[1] : a.hot[2]);
                     const int hm = __ldg(&hotm[g]);
@@ -174,14 +188,31 @@ __global__ void __launch_bounds__(256) k_staged(StagedArgs a)
                     }
                     if (hm >= 0) {
                         const float* mm = m == 0 ? a.master[0] : (m == 1 ? a.master[1] : a.master[2]);
-                        cp16(reinterpret_cast<V*>(S) + i, mm + (size_t)hm * Rp + c * 4);
+                        const float4 v0 = __ldcg(reinterpret_cast<const float4*>(mm + (size_t)hm * Rp + c * 8));
+                        const float4 v1 = __ldcg(reinterpret_cast<const float4*>(mm + (size_t)hm * Rp + c * 8 + 4));
+                        uint4 q;
+                        q.x = pack_bf16x2_rn(v0.x, v0.y);
+                        q.y = pack_bf16x2_rn(v0.z, v0.w);
+                        q.z = pack_bf16x2_rn(v1.x, v1.y);
+                        q.w = pack_bf16x2_rn(v1.z, v1.w);
+                        *reinterpret_cast<uint4*>(Sb + (size_t)r * Rp + c * 8) = q;
                     } else {
                         const unsigned short* Fm = static_cast<const unsigned short*>(
                             m == 0 ? a.A : (m == 1 ? a.B : a.C));
-                        const uint2 raw = __ldcg(reinterpret_cast<const uint2*>(Fm + (size_t)g * Rp + c * 4));
-                        reinterpret_cast<float4*>(S)[i] = bf16x4_to_float4(raw);
+                        cp16(Sb + (size_t)r * Rp + c * 8, Fm + (size_t)g * Rp + c * 8);
                     }
-                } else {
+                }
+            }
+            for (int i = tid; i < (BF ? 0 : nv); i += blockDim.x) {
+                const int r = i / vpr, c = i - r * vpr;
+                const int g = __ldg(&a.rows[h.roff + r]);
+                if constexpr (BF) {
+                    // rows stay BF16 in shared memory: 16-byte chunks of 8
+                    // elements, copied as they are; hot rows are rounded from
+                    // their FP32 masters
+                    (void)c;
+                }
+                if constexpr (!BF) {
                     if (c == 0)
                         rid[r] = g;
                     const T* Fm = r < h.nx ? FA : (r < nxy ? FB : FC);
@@ -203,15 +234,22 @@ __global__ void __launch_bounds__(256) k_staged(StagedArgs a)
                 int4 q = make_int4(0, 0, 0, 0);
                 if (act) {
                     q = ent[e];
-                    const T* sx = S + (size_t)(q.x & 0xffff) * Rp;
-                    const T* sy = S + (size_t)((unsigned)q.x >> 16) * Rp;
-                    const T* sz = S + (size_t)q.y * Rp;
+                    const size_t rx = (size_t)(q.x & 0xffff) * Rp, ry = (size_t)((unsigned)q.x >> 16) * Rp,
+                                 rz = (size_t)q.y * Rp;
 #pragma unroll
                     for (int j = 0; j < NV; j++) {
                         const int o = (j * G + gl) * VN;
-                        V vx = *reinterpret_cast<const V*>(sx + o);
-                        V vy = *reinterpret_cast<const V*>(sy + o);
-                        V vz = *reinterpret_cast<const V*>(sz + o);
+                        V vx, vy, vz;
+                        if constexpr (BF) {
+                            const unsigned short* Sb = reinterpret_cast<const unsigned short*>(smem);
+                            vx = ld_bf4(Sb + rx + o);
+                            vy = ld_bf4(Sb + ry + o);
+                            vz = ld_bf4(Sb + rz + o);
+                        } else {
+                            vx = *reinterpret_cast<const V*>(S + rx + o);
+                            vy = *reinterpret_cast<const V*>(S + ry + o);
+                            vz = *reinterpret_cast<const V*>(S + rz + o);
+                        }
                         const T* ax = reinterpret_cast<const T*>(&vx);
                         const T* ay = reinterpret_cast<const T*>(&vy);
                         const T* az = reinterpret_cast<const T*>(&vz);
@@ -246,13 +284,19 @@ __global__ void __launch_bounds__(256) k_staged(StagedArgs a)
                     const int o1 = m == 0 ? l1 : l0;
                     const int o2 = m == 2 ? l1 : l2;
                     const T er = err[e];
-                    const T* s1 = S + (size_t)o1 * Rp;
-                    const T* s2 = S + (size_t)o2 * Rp;
+                    const size_t r1 = (size_t)o1 * Rp, r2 = (size_t)o2 * Rp;
 #pragma unroll
                     for (int j = 0; j < NV; j++) {
                         const int o = (j * G + gl) * VN;
-                        V v1 = *reinterpret_cast<const V*>(s1 + o);
-                        V v2 = *reinterpret_cast<const V*>(s2 + o);
+                        V v1, v2;
+                        if constexpr (BF) {
+                            const unsigned short* Sb = reinterpret_cast<const unsigned short*>(smem);
+                            v1 = ld_bf4(Sb + r1 + o);
+                            v2 = ld_bf4(Sb + r2 + o);
+                        } else {
+                            v1 = *reinterpret_cast<const V*>(S + r1 + o);
+                            v2 = *reinterpret_cast<const V*>(S + r2 + o);
+                        }
                         const T* b1 = reinterpret_cast<const T*>(&v1);
                         const T* b2 = reinterpret_cast<const T*>(&v2);
 #pragma unroll
@@ -269,11 +313,12 @@ __global__ void __launch_bounds__(256) k_staged(StagedArgs a)
 #pragma unroll
                     for (int j = 0; j < NV; j++) {
                         const int o = (j * G + gl) * VN;
+                        const float4 own = ld_bf4(reinterpret_cast<const unsigned short*>(smem) + (size_t)row * Rp + o);
                         float4 d;
-                        d.x = w * (acc[j * VN + 0] - creg * sr[o + 0]);
-                        d.y = w * (acc[j * VN + 1] - creg * sr[o + 1]);
-                        d.z = w * (acc[j * VN + 2] - creg * sr[o + 2]);
-                        d.w = w * (acc[j * VN + 3] - creg * sr[o + 3]);
+                        d.x = w * (acc[j * VN + 0] - creg * own.x);
+                        d.y = w * (acc[j * VN + 1] - creg * own.y);
+                        d.z = w * (acc[j * VN + 2] - creg * own.z);
+                        d.w = w * (acc[j * VN + 3] - creg * own.w);
                         if (hm >= 0) {
                             float* mm = m == 0 ? a.master[0] : (m == 1 ? a.master[1] : a.master[2]);
                             red_v(mm + (size_t)hm * Rp + o, d);
@@ -330,47 +375,63 @@ void pick(int R, int& G, int& NV)
 }
 
 template <typename T, bool BF>
-const void* kernel_for(int R)
+const void* kernel_for(int R, int G, int NV)
 {
-    int G, NV;
-    pick<T>(R, G, NV);
+    if (G <= 0)
+        pick<T>(R, G, NV);
 #define BTC_KS(g, nv)                                 \
     if (G == g && NV == nv)                           \
         return (const void*)&k_staged<T, g, nv, BF>;
     BTC_KS(1, 1) BTC_KS(2, 1) BTC_KS(4, 1) BTC_KS(8, 1) BTC_KS(16, 1) BTC_KS(32, 1) BTC_KS(32, 2)
+    BTC_KS(1, 2) BTC_KS(2, 2) BTC_KS(4, 2) BTC_KS(8, 2) BTC_KS(16, 2)
 #undef BTC_KS
     return nullptr;
 }
 
-const void* kernel_for_dtype(int dtype, int R)
+const void* kernel_for_dtype(int dtype, int R, int G, int NV)
 {
     if (dtype == 1)
-        return kernel_for<double, false>(R);
+        return kernel_for<double, false>(R, G, NV);
     if (dtype == 2)
-        return kernel_for<float, true>(R);
-    return kernel_for<float, false>(R);
+        return kernel_for<float, true>(R, G, NV);
+    return kernel_for<float, false>(R, G, NV);
 }
 
 }  // namespace
 
 size_t staged_smem_bytes(int dtype, int Rp, int cap, int wave)
 {
-    return StagedLayout(dtype == 1 ? 8 : 4, Rp, cap, wave).total;
+    return StagedLayout(dtype == 1 ? 8 : (dtype == 2 ? 2 : 4), Rp, cap, wave).total;
 }
 
 int staged_cap_for(int dtype, int Rp, int wave, int ctas_per_sm, size_t smem_per_sm, size_t smem_per_block)
 {
-    size_t es = dtype == 1 ? 8 : 4;
+    size_t es = dtype == 1 ? 8 : (dtype == 2 ? 2 : 4);
     size_t budget = std::min(smem_per_block, smem_per_sm / (size_t)std::max(1, ctas_per_sm) - 1024);
-    int cap = (int)std::min<size_t>(65535, budget / ((size_t)Rp * es + 4));
+    int cap = (int)std::min<size_t>(65535, budget / ((size_t)Rp * es + 8));
     while (cap > 0 && staged_smem_bytes(dtype, Rp, cap, wave) > budget)
         cap--;
     return cap;
 }
 
+int staged_vector_width(int dtype) { return dtype == 1 ? 2 : 4; }
+
+void staged_default_shape(int dtype, int R, int* G, int* NV)
+{
+    if (dtype == 1)
+        pick<double>(R, *G, *NV);
+    else
+        pick<float>(R, *G, *NV);
+}
+
+bool staged_shape_exists(int dtype, int R, int G, int NV)
+{
+    return G > 0 && kernel_for_dtype(dtype, R, G, NV) != nullptr;
+}
+
 cudaError_t launch_staged(int dtype, const StagedArgs& a, int grid, int block, cudaStream_t st)
 {
-    const void* fn = kernel_for_dtype(dtype, a.R);
+    const void* fn = kernel_for_dtype(dtype, a.R, a.G, a.NV);
     if (!fn)
         return cudaErrorInvalidValue;
     size_t smem = staged_smem_bytes(dtype, a.Rp, a.cap, a.wave);
@@ -381,9 +442,22 @@ cudaError_t launch_staged(int dtype, const StagedArgs& a, int grid, int block, c
     return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, st);
 }
 
+int staged_blocks_per_sm_shape(int dtype, int R, int G, int NV, int block, size_t smem)
+{
+    const void* fn = kernel_for_dtype(dtype, R, G, NV);
+    if (!fn)
+        return 0;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, block, smem) != cudaSuccess)
+        return 0;
+    return n;
+}
+
 int staged_blocks_per_sm(int dtype, int R, int block, size_t smem)
 {
-    const void* fn = kernel_for_dtype(dtype, R);
+    const void* fn = kernel_for_dtype(dtype, R, 0, 0);
     if (!fn)
         return 0;
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)

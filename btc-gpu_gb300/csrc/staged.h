@@ -34,19 +34,23 @@ struct StagedArgs {
     unsigned seed;           // stochastic-rounding stream of this epoch
     int* status;             // set to 1 when a rounding compare-and-swap gives up
     unsigned* tile_ns;       // when set: nanoseconds each tile took (globaltimer)
+    int G, NV;               // lane-group shape; 0 = the default for the rank
 };
 
 // Shared-memory layout of one CTA: S rows | entries | errors | row ids and
 // master slots | CSR.
 // Every region that receives 16-byte copies starts on a 16-byte boundary.
+// es = bytes of one staged row element (8 FP64, 4 FP32, 2 BF16); errors are
+// kept in the compute type (8 for FP64, else 4).
 struct StagedLayout {
     size_t ent, err, rid, csr, total;
     __host__ __device__ StagedLayout(size_t es, int Rp, int cap, int wave)
     {
         auto al = [](size_t v) { return (v + 15) & ~(size_t)15; };
+        const size_t ee = es == 8 ? 8 : 4;
         ent = al((size_t)cap * Rp * es);
         err = al(ent + (size_t)wave * 16);
-        rid = al(err + (size_t)wave * es);
+        rid = al(err + (size_t)wave * ee);
         csr = al(rid + (size_t)cap * 8);
         total = al(csr + (3 * (size_t)wave + 8) * 2);
     }
@@ -57,6 +61,12 @@ size_t staged_smem_bytes(int dtype, int Rp, int cap, int wave);
 // Largest cap that fits `ctas_per_sm` CTAs on one SM.
 int staged_cap_for(int dtype, int Rp, int wave, int ctas_per_sm, size_t smem_per_sm, size_t smem_per_block);
 cudaError_t launch_staged(int dtype, const StagedArgs& a, int grid, int block, cudaStream_t st);
+// Lane-group shapes: G lanes per entry, NV 16-byte vectors per lane per row
+// (G * NV * vector width must cover the padded rank).
+int staged_vector_width(int dtype);
+void staged_default_shape(int dtype, int R, int* G, int* NV);
+bool staged_shape_exists(int dtype, int R, int G, int NV);
 int staged_blocks_per_sm(int dtype, int R, int block, size_t smem);
+int staged_blocks_per_sm_shape(int dtype, int R, int G, int NV, int block, size_t smem);
 
 }  // namespace btc

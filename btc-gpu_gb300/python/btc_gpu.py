@@ -111,6 +111,7 @@ SIGNATURES = {
     "btc_mlp_train": ([P, P, P, I64, I32, ctypes.c_float, P], ctypes.c_int),
     "btc_mlp_predict": ([P, P, I64, P], ctypes.c_int),
     "btc_ctx_learn_work_units": ([P, P, I32, I32, P], ctypes.c_int),
+    "btc_ctx_autotune": ([P, I32, P], ctypes.c_int),
     "btc_ctx_slot_tiles": ([P, P, P], ctypes.c_int),
     "btc_ctx_set_work_units": ([P, P, I32], ctypes.c_int),
     "btc_ctx_tile_features": ([P, P], ctypes.c_int),
@@ -225,6 +226,12 @@ class LearnReport(ctypes.Structure):
     _fields_ = [("plain_ms", ctypes.c_double), ("learned_ms", ctypes.c_double),
                 ("model_loss", ctypes.c_double), ("model_r2", ctypes.c_double),
                 ("samples", ctypes.c_int64), ("units", ctypes.c_int32), ("kept", ctypes.c_int32)]
+
+
+class AutotuneReport(ctypes.Structure):
+    _fields_ = [("lanes_per_entry", ctypes.c_int32), ("vectors_per_lane", ctypes.c_int32),
+                ("ctas_per_sm", ctypes.c_int32), ("candidates", ctypes.c_int32),
+                ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double)]
 
 
 class MLP:
@@ -435,6 +442,11 @@ class Context:
         r = LearnReport()
         _ck(_lib().btc_ctx_learn_work_units(self._h, model.handle, train_steps, judge_epochs, ctypes.byref(r)),
             "btc_ctx_learn_work_units")
+        return r
+
+    def autotune(self, epochs_per_candidate=2):
+        r = AutotuneReport()
+        _ck(_lib().btc_ctx_autotune(self._h, epochs_per_candidate, ctypes.byref(r)), "btc_ctx_autotune")
         return r
 
     def train_epoch_profiled(self):

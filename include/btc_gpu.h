@@ -241,6 +241,23 @@ typedef struct btc_learn_report {
 btc_status btc_ctx_learn_work_units(btc_ctx *ctx, btc_mlp *model, int32_t train_steps, int32_t judge_epochs,
                                     btc_learn_report *report);
 
+/* ---- autotuner -------------------------------------------------------------
+ * No counterpart in the reference.  Times the staged kernel on the context's
+ * own tiles for every lane-group shape (lanes per entry x 16-byte vectors per
+ * lane, same row coverage) and every CTAs-per-SM count the shared memory
+ * allows, epochs_per_candidate training epochs each, and keeps the fastest.
+ * The tile capacity (rows per tile for the rank) is fixed when the context
+ * is created (cfg.ctas_per_sm). */
+typedef struct btc_autotune_report {
+    int32_t lanes_per_entry;
+    int32_t vectors_per_lane;
+    int32_t ctas_per_sm;
+    int32_t candidates;
+    double best_ms;       /* mean epoch time of the choice */
+    double default_ms;    /* mean epoch time of the default shape and grid */
+} btc_autotune_report;
+btc_status btc_ctx_autotune(btc_ctx *ctx, int32_t epochs_per_candidate, btc_autotune_report *report);
+
 /* Device stream the context launches on (a cudaStream_t). */
 void *btc_ctx_stream(btc_ctx *ctx);
 btc_status btc_ctx_destroy(btc_ctx *ctx);
