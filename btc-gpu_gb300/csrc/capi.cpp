@@ -760,6 +760,40 @@ static btc::SgdArgs sgd_args(btc_ctx* c)
     return a;
 }
 
+static btc::StagedArgs staged_args(btc_ctx* c)
+{
+    btc::StagedArgs s{};
+    s.tiles = c->tiles;
+    s.slot_tile0 = c->slot_tile0;
+    s.slot_ntiles = c->slot_ntiles;
+    s.slot_coe = c->slot_coe;
+    s.nslots = c->nslots;
+    s.unit_off = c->unit_off;
+    s.nunits = c->nunits;
+    s.ent = c->tent;
+    s.csr = c->tcsr;
+    s.segs = c->tsegs;
+    s.rows = c->trows;
+    s.val64 = c->tval64;
+    s.A = c->F[0];
+    s.B = c->F[1];
+    s.C = c->F[2];
+    s.R = c->R;
+    s.Rp = c->Rp;
+    s.reg = c->cfg.reg;
+    s.cap = c->st_cap;
+    s.wave = c->st_wave;
+    s.counter = c->counter;
+    s.G = c->st_G;
+    s.NV = c->st_NV;
+    s.status = c->status;
+    for (int a = 0; a < 3; a++) {
+        s.master[a] = c->master[a];
+        s.hot[a] = c->hot_map[a];
+    }
+    return s;
+}
+
 static btc_status enqueue_epoch(btc_ctx* c, int* launches)
 {
     btc::SgdArgs a = sgd_args(c);
@@ -775,36 +809,8 @@ static btc_status enqueue_epoch(btc_ctx* c, int* launches)
         }
     } else if (c->mode == BTC_MODE_STAGED) {
         if (c->nslots > 0) {
-            btc::StagedArgs s{};
-            s.tiles = c->tiles;
-            s.slot_tile0 = c->slot_tile0;
-            s.slot_ntiles = c->slot_ntiles;
-            s.slot_coe = c->slot_coe;
-            s.nslots = c->nslots;
-            s.unit_off = c->unit_off;
-            s.nunits = c->nunits;
-            s.ent = c->tent;
-            s.csr = c->tcsr;
-            s.segs = c->tsegs;
-            s.rows = c->trows;
-            s.val64 = c->tval64;
-            s.A = c->F[0];
-            s.B = c->F[1];
-            s.C = c->F[2];
-            s.R = c->R;
-            s.Rp = c->Rp;
-            s.reg = c->cfg.reg;
-            s.cap = c->st_cap;
-            s.wave = c->st_wave;
-            s.counter = c->counter;
-            s.G = c->st_G;
-            s.NV = c->st_NV;
-            s.status = c->status;
+            btc::StagedArgs s = staged_args(c);
             s.tile_ns = c->profile_next ? c->tile_ns : nullptr;
-            for (int a = 0; a < 3; a++) {
-                s.master[a] = c->master[a];
-                s.hot[a] = c->hot_map[a];
-            }
             c->epoch++;
             s.seed = (c->epoch * 0x9E3779B9u) ^ 0x5BD1E995u;
             CK(cudaMemsetAsync(c->counter, 0, sizeof(int), c->stream));
@@ -1201,6 +1207,202 @@ btc_status btc_train_epoch_host(btc_ctx* c, double* A, double* B, double* C, btc
         if ((rc = btc_ctx_get_factors(c, m, H[m])))
             return rc;
     return BTC_OK;
+}
+
+struct btc_batch {
+    std::vector<btc_ctx*> ctx;
+    int dtype = 0, device = 0, nitems = 0, grid = 0;
+    size_t smem = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    btc::StagedArgs* args = nullptr;
+    int2* items = nullptr;
+    int* counter = nullptr;
+    unsigned* seed = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t updates = 0;
+    int launches = 0;
+};
+
+btc_status btc_batch_destroy(btc_batch* b)
+{
+    if (!b)
+        return BTC_OK;
+    cudaSetDevice(b->device);
+    if (b->stream)
+        cudaStreamSynchronize(b->stream);
+    if (b->exec)
+        cudaGraphExecDestroy(b->exec);
+    if (b->graph)
+        cudaGraphDestroy(b->graph);
+    free_dev(b->args);
+    free_dev(b->items);
+    free_dev(b->counter);
+    free_dev(b->seed);
+    if (b->ev0)
+        cudaEventDestroy(b->ev0);
+    if (b->ev1)
+        cudaEventDestroy(b->ev1);
+    if (b->stream)
+        cudaStreamDestroy(b->stream);
+    delete b;
+    return BTC_OK;
+}
+
+static btc_status batch_build(btc_batch* b)
+{
+    CK(cudaSetDevice(b->device));
+    CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&b->ev0));
+    CK(cudaEventCreate(&b->ev1));
+    const int n = (int)b->ctx.size();
+    std::vector<btc::StagedArgs> args((size_t)n);
+    std::vector<std::pair<double, int2>> order;
+    for (int t = 0; t < n; t++) {
+        btc_ctx* c = b->ctx[(size_t)t];
+        args[(size_t)t] = staged_args(c);
+        args[(size_t)t].seed = 0x2545F491u * (unsigned)(t + 1);
+        b->smem = std::max(b->smem, btc::staged_smem_bytes(b->dtype, c->Rp, c->st_cap, c->st_wave));
+        b->updates += c->updates;
+        // interleave: unit u of tensor t is placed at its progress fraction
+        for (int u = 0; u < c->nunits; u++)
+            order.push_back({((double)u + 0.5) / (double)c->nunits, make_int2(t, u)});
+    }
+    std::stable_sort(order.begin(), order.end(),
+                     [](const std::pair<double, int2>& x, const std::pair<double, int2>& y) { return x.first < y.first; });
+    std::vector<int2> items;
+    items.reserve(order.size());
+    for (auto& o : order)
+        items.push_back(o.second);
+    b->nitems = (int)items.size();
+    CK(cudaMalloc((void**)&b->seed, sizeof(unsigned)));
+    CK(cudaMemsetAsync(b->seed, 0, sizeof(unsigned), b->stream));
+    for (auto& a : args)
+        a.seed_ptr = b->seed;
+    btc_status rc;
+    if ((rc = upload((void**)&b->args, args.data(), args.size() * sizeof(btc::StagedArgs), b->stream)))
+        return rc;
+    if ((rc = upload((void**)&b->items, items.data(), items.size() * sizeof(int2), b->stream)))
+        return rc;
+    CK(cudaMalloc((void**)&b->counter, sizeof(int)));
+    int occ = btc::staged_multi_blocks_per_sm(b->dtype, b->smem);
+    if (occ <= 0)
+        return BTC_ERR_UNSUPPORTED;
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, b->device));
+    b->grid = prop.multiProcessorCount * occ;
+    CK(cudaStreamSynchronize(b->stream));
+    return BTC_OK;
+}
+
+btc_status btc_batch_create(btc_ctx* const* ctxs, int32_t n, btc_batch** out)
+{
+    if (!ctxs || n <= 0 || !out)
+        return BTC_ERR_ARG;
+    *out = nullptr;
+    const int dtype = ctxs[0]->dtype, device = ctxs[0]->cfg.device;
+    for (int i = 0; i < n; i++) {
+        const btc_ctx* c = ctxs[i];
+        if (!c || c->mode != BTC_MODE_STAGED || c->dtype != dtype || c->cfg.device != device || c->R > 128)
+            return BTC_ERR_ARG;
+    }
+    if (dtype == BTC_DTYPE_F64)
+        return BTC_ERR_UNSUPPORTED;
+    btc_batch* b = new (std::nothrow) btc_batch();
+    if (!b)
+        return BTC_ERR_ALLOC;
+    b->ctx.assign(ctxs, ctxs + n);
+    b->dtype = dtype;
+    b->device = device;
+    btc_status rc;
+    try {
+        rc = batch_build(b);
+    } catch (const std::bad_alloc&) {
+        rc = BTC_ERR_ALLOC;
+    }
+    if (rc) {
+        btc_batch_destroy(b);
+        return rc;
+    }
+    *out = b;
+    return BTC_OK;
+}
+
+static btc_status batch_enqueue(btc_batch* b, int* launches)
+{
+    int n = 0;
+    CK(cudaMemsetAsync(b->counter, 0, sizeof(int), b->stream));
+    CK(btc::launch_staged_multi(b->dtype, b->args, b->items, b->nitems, b->counter, b->smem, b->grid, b->stream));
+    n++;
+    if (b->dtype == BTC_DTYPE_BF16) {
+        for (btc_ctx* c : b->ctx)
+            for (int a = 0; a < 3; a++)
+                if (c->nhot[a] > 0) {
+                    CK(btc::launch_master(2, nullptr, nullptr, c->master[a], c->F[a], c->hot_rows[a], c->nhot[a],
+                                          c->R, c->Rp, b->stream));
+                    n++;
+                }
+    }
+    CK(btc::launch_seed_step(b->seed, b->stream));
+    n++;
+    if (launches)
+        *launches = n;
+    return BTC_OK;
+}
+
+btc_status btc_batch_train_epochs(btc_batch* b, int32_t epochs, int32_t use_graph, btc_epoch_stats* st)
+{
+    if (!b || epochs < 0)
+        return BTC_ERR_ARG;
+    CK(cudaSetDevice(b->device));
+    int per = 0;
+    if (use_graph && !b->exec) {
+        CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        btc_status rc = batch_enqueue(b, &per);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+        if (rc)
+            return rc;
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaStreamEndCapture");
+        b->graph = g;
+        CK(cudaGraphInstantiate(&b->exec, g, 0));
+        b->launches = per;
+    }
+    CK(cudaEventRecord(b->ev0, b->stream));
+    int total = 0;
+    for (int e = 0; e < epochs; e++) {
+        if (use_graph) {
+            CK(cudaGraphLaunch(b->exec, b->stream));
+            total += b->launches;
+        } else {
+            btc_status rc = batch_enqueue(b, &per);
+            if (rc)
+                return rc;
+            total += per;
+        }
+    }
+    CK(cudaEventRecord(b->ev1, b->stream));
+    CK(cudaEventSynchronize(b->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    btc_status rs = BTC_OK;
+    int word = 0;
+    for (btc_ctx* c : b->ctx) {
+        int w = 0;
+        btc_status r1 = check_status(c, &w);
+        if (r1 && !rs)
+            rs = r1;
+        word |= w;
+    }
+    if (st) {
+        st->kernel_ms = ms;
+        st->updates = b->updates * (int64_t)epochs;
+        st->launches = total;
+        st->device_status = word;
+    }
+    return rs;
 }
 
 }  // extern "C"

@@ -473,12 +473,20 @@ __global__ void k_master_refresh(const float* master, unsigned short* dst, const
     }
 }
 
+__global__ void k_seed_step(unsigned* p) { *p += 0x9E3779B9u; }
+
 int grid_for(long long n)
 {
     return (int)std::min<long long>(4096, (n + 255) / 256 + 1);
 }
 
 }  // namespace
+
+cudaError_t launch_seed_step(unsigned* p, cudaStream_t st)
+{
+    k_seed_step<<<1, 1, 0, st>>>(p);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_master(int op, const double* src, double* dst, float* master, void* bf16, const int* hot_rows,
                           int nhot, int R, int Rp, cudaStream_t st)

@@ -123,14 +123,16 @@ __device__ __forceinline__ void cp16(void* smem_dst, const void* gsrc)
 }
 __device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-template <typename T, int G, int NV, bool BF>
-__global__ void __launch_bounds__(256, 4) k_staged(StagedArgs a)
+// One work unit of one tensor: slots [unit_off[unit], unit_off[unit+1]),
+// tile by tile.  MASK allows a row shorter than G*NV*VN elements (the lanes
+// past the padded rank stay idle), so one shape serves every rank of a batch.
+template <typename T, int G, int NV, bool BF, bool MASK>
+__device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned char* smem)
 {
     using V = typename SV<T>::V;
     constexpr int VN = SV<T>::N;
     constexpr int EPW = 32 / G;
     constexpr int E = NV * VN;
-    extern __shared__ __align__(16) unsigned char smem[];
     const int Rp = a.Rp;
     const StagedLayout L(BF ? 2 : sizeof(T), Rp, a.cap, a.wave);
     T* S = reinterpret_cast<T*>(smem);
@@ -138,8 +140,6 @@ __global__ void __launch_bounds__(256, 4) k_staged(StagedArgs a)
     T* err = reinterpret_cast<T*>(smem + L.err);
     int* rid = reinterpret_cast<int*>(smem + L.rid);
     unsigned short* csr = reinterpret_cast<unsigned short*>(smem + L.csr);
-    __shared__ int s_slot;
-
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
     const int sub = lane / G, gl = lane % G;
@@ -149,15 +149,8 @@ __global__ void __launch_bounds__(256, 4) k_staged(StagedArgs a)
     const T reg = (T)a.reg;
     const int vpr = Rp / VN;
     const T* coe = static_cast<const T*>(a.slot_coe);
-
-    for (;;) {
-        __syncthreads();
-        if (tid == 0)
-            s_slot = atomicAdd(a.counter, 1);
-        __syncthreads();
-        const int unit = s_slot;
-        if (unit >= a.nunits)
-            break;
+    const unsigned seed = a.seed_ptr ? (a.seed ^ *a.seed_ptr) : a.seed;
+    {
         const int u0 = __ldg(&a.unit_off[unit]), u1 = __ldg(&a.unit_off[unit + 1]);
       for (int slot = u0; slot < u1; slot++) {
         const T cx = coe[3 * slot], cy = coe[3 * slot + 1], cz = coe[3 * slot + 2];
@@ -239,6 +232,8 @@ __global__ void __launch_bounds__(256, 4) k_staged(StagedArgs a)
 #pragma unroll
                     for (int j = 0; j < NV; j++) {
                         const int o = (j * G + gl) * VN;
+                        if (MASK && o >= Rp)
+                            continue;
                         V vx, vy, vz;
                         if constexpr (BF) {
                             const unsigned short* Sb = reinterpret_cast<const unsigned short*>(smem);
@@ -288,6 +283,8 @@ __global__ void __launch_bounds__(256, 4) k_staged(StagedArgs a)
 #pragma unroll
                     for (int j = 0; j < NV; j++) {
                         const int o = (j * G + gl) * VN;
+                        if (MASK && o >= Rp)
+                            continue;
                         V v1, v2;
                         if constexpr (BF) {
                             const unsigned short* Sb = reinterpret_cast<const unsigned short*>(smem);
@@ -313,6 +310,8 @@ __global__ void __launch_bounds__(256, 4) k_staged(StagedArgs a)
 #pragma unroll
                     for (int j = 0; j < NV; j++) {
                         const int o = (j * G + gl) * VN;
+                        if (MASK && o >= Rp)
+                            continue;
                         const float4 own = ld_bf4(reinterpret_cast<const unsigned short*>(smem) + (size_t)row * Rp + o);
                         float4 d;
                         d.x = w * (acc[j * VN + 0] - creg * own.x);
@@ -324,8 +323,8 @@ __global__ void __launch_bounds__(256, 4) k_staged(StagedArgs a)
                             red_v(mm + (size_t)hm * Rp + o, d);
                         } else {
                             unsigned* wp = reinterpret_cast<unsigned*>(Fm + (size_t)g * Rp + o);
-                            const unsigned rnd0 = mix3(a.seed ^ (unsigned)(m * 0x68E31DA4u), (unsigned)g, (unsigned)o);
-                            const unsigned rnd1 = mix3(a.seed ^ (unsigned)(m * 0x68E31DA4u), (unsigned)g, (unsigned)o + 2);
+                            const unsigned rnd0 = mix3(seed ^ (unsigned)(m * 0x68E31DA4u), (unsigned)g, (unsigned)o);
+                            const unsigned rnd1 = mix3(seed ^ (unsigned)(m * 0x68E31DA4u), (unsigned)g, (unsigned)o + 2);
                             bool ok = true;
                             if (d.x != 0.f || d.y != 0.f)
                                 ok &= add_pair_sr(wp, d.x, d.y, rnd0);
@@ -340,6 +339,8 @@ __global__ void __launch_bounds__(256, 4) k_staged(StagedArgs a)
 #pragma unroll
                     for (int j = 0; j < NV; j++) {
                         const int o = (j * G + gl) * VN;
+                        if (MASK && o >= Rp)
+                            continue;
                         V d;
                         T* dd = reinterpret_cast<T*>(&d);
 #pragma unroll
@@ -359,6 +360,47 @@ __global__ void __launch_bounds__(256, 4) k_staged(StagedArgs a)
             }
         }
       }
+    }
+}
+
+template <typename T, int G, int NV, bool BF>
+__global__ void __launch_bounds__(256, 4) k_staged(StagedArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_unit;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0)
+            s_unit = atomicAdd(a.counter, 1);
+        __syncthreads();
+        const int unit = s_unit;
+        if (unit >= a.nunits)
+            break;
+        run_unit<T, G, NV, BF, false>(a, unit, smem);
+    }
+}
+
+// Many tensors in one persistent launch: work items (tensor, unit) are taken
+// from one counter; each tensor brings its own arguments (rank, tiles,
+// factors, weights).  8 lanes per entry, up to 4 vectors per lane: ranks up to
+// 128 (FP32/BF16), shorter rows leave lanes idle.
+template <bool BF>
+__global__ void __launch_bounds__(256, 4) k_staged_multi(const StagedArgs* __restrict__ tensors,
+                                                         const int2* __restrict__ items, int nitems, int* counter)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_item;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0)
+            s_item = atomicAdd(counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= nitems)
+            break;
+        const int2 w = __ldg(&items[it]);
+        const StagedArgs a = tensors[w.x];
+        run_unit<float, 8, 4, BF, true>(a, w.y, smem);
     }
 }
 
@@ -427,6 +469,30 @@ void staged_default_shape(int dtype, int R, int* G, int* NV)
 bool staged_shape_exists(int dtype, int R, int G, int NV)
 {
     return G > 0 && kernel_for_dtype(dtype, R, G, NV) != nullptr;
+}
+
+cudaError_t launch_staged_multi(int dtype, const StagedArgs* tensors, const int2* items, int nitems, int* counter,
+                                size_t smem, int grid, cudaStream_t st)
+{
+    const void* fn = dtype == 2 ? (const void*)&k_staged_multi<true> : (const void*)&k_staged_multi<false>;
+    if (dtype == 1)
+        return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    void* args[] = {(void*)&tensors, (void*)&items, (void*)&nitems, (void*)&counter};
+    return cudaLaunchKernel(fn, dim3(grid), dim3(256), args, smem, st);
+}
+
+int staged_multi_blocks_per_sm(int dtype, size_t smem)
+{
+    const void* fn = dtype == 2 ? (const void*)&k_staged_multi<true> : (const void*)&k_staged_multi<false>;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, 256, smem) != cudaSuccess)
+        return 0;
+    return n;
 }
 
 cudaError_t launch_staged(int dtype, const StagedArgs& a, int grid, int block, cudaStream_t st)

@@ -35,6 +35,7 @@ struct StagedArgs {
     int* status;             // set to 1 when a rounding compare-and-swap gives up
     unsigned* tile_ns;       // when set: nanoseconds each tile took (globaltimer)
     int G, NV;               // lane-group shape; 0 = the default for the rank
+    const unsigned* seed_ptr;  // when set, the rounding stream is seed ^ *seed_ptr (graph replays)
 };
 
 // Shared-memory layout of one CTA: S rows | entries | errors | row ids and
@@ -61,6 +62,11 @@ size_t staged_smem_bytes(int dtype, int Rp, int cap, int wave);
 // Largest cap that fits `ctas_per_sm` CTAs on one SM.
 int staged_cap_for(int dtype, int Rp, int wave, int ctas_per_sm, size_t smem_per_sm, size_t smem_per_block);
 cudaError_t launch_staged(int dtype, const StagedArgs& a, int grid, int block, cudaStream_t st);
+// Many tensors in one launch: `tensors` (device) holds each tensor's
+// arguments, `items` (device) the (tensor, unit) work list.
+cudaError_t launch_staged_multi(int dtype, const StagedArgs* tensors, const int2* items, int nitems, int* counter,
+                                size_t smem, int grid, cudaStream_t st);
+int staged_multi_blocks_per_sm(int dtype, size_t smem);
 // Lane-group shapes: G lanes per entry, NV 16-byte vectors per lane per row
 // (G * NV * vector width must cover the padded rank).
 int staged_vector_width(int dtype);

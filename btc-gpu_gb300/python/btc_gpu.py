@@ -112,6 +112,9 @@ SIGNATURES = {
     "btc_mlp_predict": ([P, P, I64, P], ctypes.c_int),
     "btc_ctx_learn_work_units": ([P, P, I32, I32, P], ctypes.c_int),
     "btc_ctx_autotune": ([P, I32, P], ctypes.c_int),
+    "btc_batch_create": ([P, I32, P], ctypes.c_int),
+    "btc_batch_train_epochs": ([P, I32, I32, P], ctypes.c_int),
+    "btc_batch_destroy": ([P], ctypes.c_int),
     "btc_ctx_slot_tiles": ([P, P, P], ctypes.c_int),
     "btc_ctx_set_work_units": ([P, P, I32], ctypes.c_int),
     "btc_ctx_tile_features": ([P, P], ctypes.c_int),
@@ -284,6 +287,33 @@ class MLP:
     def close(self):
         if getattr(self, "_h", None):
             _lib().btc_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Several staged contexts trained as one persistent launch per epoch."""
+
+    def __init__(self, contexts):
+        self.contexts = list(contexts)
+        arr = (ctypes.c_void_p * len(self.contexts))(*[c.handle.value for c in self.contexts])
+        h = ctypes.c_void_p()
+        _ck(_lib().btc_batch_create(arr, len(self.contexts), ctypes.byref(h)), "btc_batch_create")
+        self._h = h
+
+    def train_epochs(self, n, graph=True):
+        st = EpochStats()
+        _ck(_lib().btc_batch_train_epochs(self._h, n, 1 if graph else 0, ctypes.byref(st)), "btc_batch_train_epochs")
+        return st
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib().btc_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -258,6 +258,21 @@ typedef struct btc_autotune_report {
 } btc_autotune_report;
 btc_status btc_ctx_autotune(btc_ctx *ctx, int32_t epochs_per_candidate, btc_autotune_report *report);
 
+/* ---- many tensors in one launch ------------------------------------------
+ * No counterpart in the reference (its binary trains one tensor per run).
+ * A batch runs the epochs of several staged contexts (same device, FP32 or
+ * BF16 each the same) as ONE persistent kernel launch: the contexts' work
+ * units are interleaved in proportion to their sizes into one list that all
+ * CTAs drain from a single counter, every tensor with its own rank, tiles and
+ * factors.  With use_graph the epoch (counter reset, the launch, BF16 master
+ * refreshes, rounding-seed step) is captured once as a CUDA graph and
+ * replayed.  The contexts must outlive the batch; btc_eval on each context
+ * still works between batch epochs. */
+typedef struct btc_batch btc_batch;
+btc_status btc_batch_create(btc_ctx *const *ctxs, int32_t n, btc_batch **out);
+btc_status btc_batch_train_epochs(btc_batch *b, int32_t epochs, int32_t use_graph, btc_epoch_stats *stats);
+btc_status btc_batch_destroy(btc_batch *b);
+
 /* Device stream the context launches on (a cudaStream_t). */
 void *btc_ctx_stream(btc_ctx *ctx);
 btc_status btc_ctx_destroy(btc_ctx *ctx);
