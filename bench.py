@@ -451,6 +451,12 @@ def run_c4(args):
     res["batched_graph"] = upd * args.steps / (st.kernel_ms / 1e3)
     st_ng = b.train_epochs(args.steps, graph=False)
     res["batched_no_graph"] = upd * args.steps / (st_ng.kernel_ms / 1e3)
+    # test RMSE after the same number of epochs from the same init, batched vs plain
+    epochs_cmp = 10
+    for c, t in zip(cs, tensors):
+        for m in range(3):
+            c.set_factors(m, t[3][m])
+    b.train_epochs(epochs_cmp, graph=True)
     rm_batch = [c.eval(bg.TEST).rmse for c in cs]
     b.close()
     # the same kernel, one launch per tensor, one tensor after another
@@ -463,12 +469,13 @@ def run_c4(args):
         c.close()
     # the plain FP32 path run sequentially per tensor
     cp = contexts(bg.F32, bg.HOGWILD)
+    for c in cp:
+        c.train_epochs(epochs_cmp)
+    rm_plain = [c.eval(bg.TEST).rmse for c in cp]
     pl_ms = 0.0
     for c in cp:
-        c.train_epochs(1)
         pl_ms += c.train_epochs(args.steps).kernel_ms
     res["sequential_plain_fp32"] = upd * args.steps / (pl_ms / 1e3)
-    rm_plain = [c.eval(bg.TEST).rmse for c in cp]
     for c in cp:
         c.close()
     line = {"metric": "aggregate nnz-updates/s, 64 tensors", "value": res["batched_graph"], "unit": "updates/s",

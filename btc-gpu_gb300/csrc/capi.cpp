@@ -1263,6 +1263,15 @@ static btc_status batch_build(btc_batch* b)
         btc_ctx* c = b->ctx[(size_t)t];
         args[(size_t)t] = staged_args(c);
         args[(size_t)t].seed = 0x2545F491u * (unsigned)(t + 1);
+        // lanes per entry for the batched kernel: the rank's 16-byte vectors,
+        // at most 8 lanes (and at most 4 vectors per lane)
+        const int vecs = c->Rp / 4;
+        int G = 1;
+        while (G < 8 && G < vecs)
+            G *= 2;
+        if ((vecs + G - 1) / G > 4)
+            return BTC_ERR_UNSUPPORTED;
+        args[(size_t)t].G = G;
         b->smem = std::max(b->smem, btc::staged_smem_bytes(b->dtype, c->Rp, c->st_cap, c->st_wave));
         b->updates += c->updates;
         // interleave: unit u of tensor t is placed at its progress fraction

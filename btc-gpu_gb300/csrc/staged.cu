@@ -126,12 +126,16 @@ __device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;
 // One work unit of one tensor: slots [unit_off[unit], unit_off[unit+1]),
 // tile by tile.  MASK allows a row shorter than G*NV*VN elements (the lanes
 // past the padded rank stay idle), so one shape serves every rank of a batch.
-template <typename T, int G, int NV, bool BF, bool MASK>
+template <typename T, int GC, int NV, bool BF, bool MASK>
 __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned char* smem)
 {
     using V = typename SV<T>::V;
     constexpr int VN = SV<T>::N;
-    constexpr int EPW = 32 / G;
+    // GC > 0: lanes per entry fixed at compile time; GC == 0: taken from the
+    // tensor's arguments (a.G, a power of two <= 8) so that a batch of tensors
+    // of different ranks keeps every lane busy
+    const int G = GC > 0 ? GC : a.G;
+    const int EPW = 32 / G;
     constexpr int E = NV * VN;
     const int Rp = a.Rp;
     const StagedLayout L(BF ? 2 : sizeof(T), Rp, a.cap, a.wave);
@@ -253,7 +257,6 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
                             p = fma(ax[k], ay[k] * az[k], p);
                     }
                 }
-#pragma unroll
                 for (int o = G / 2; o > 0; o >>= 1)
                     p += __shfl_xor_sync(FULL, p, o);
                 if (act && gl == 0)
@@ -382,8 +385,8 @@ __global__ void __launch_bounds__(256, 4) k_staged(StagedArgs a)
 
 // Many tensors in one persistent launch: work items (tensor, unit) are taken
 // from one counter; each tensor brings its own arguments (rank, tiles,
-// factors, weights).  8 lanes per entry, up to 4 vectors per lane: ranks up to
-// 128 (FP32/BF16), shorter rows leave lanes idle.
+// factors, weights, lanes per entry).  Up to 8 lanes per entry and 4 vectors
+// per lane: ranks up to 128 (FP32/BF16).
 template <bool BF>
 __global__ void __launch_bounds__(256, 4) k_staged_multi(const StagedArgs* __restrict__ tensors,
                                                          const int2* __restrict__ items, int nitems, int* counter)
@@ -400,7 +403,7 @@ __global__ void __launch_bounds__(256, 4) k_staged_multi(const StagedArgs* __res
             break;
         const int2 w = __ldg(&items[it]);
         const StagedArgs a = tensors[w.x];
-        run_unit<float, 8, 4, BF, true>(a, w.y, smem);
+        run_unit<float, 0, 4, BF, true>(a, w.y, smem);
     }
 }
 
