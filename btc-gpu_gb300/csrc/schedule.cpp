@@ -106,7 +106,19 @@ void finish_block_codes(BlockRec& b)
     }
 }
 
-btc_status blocking(const int32_t* xyz, int64_t n, int I, int J, int K, int bs, Schedule& s)
+// Route one entry from `node` down to a leaf with bucket codes pc at global
+// levels g (search_block, block.cu:64-88).
+inline int route(const std::vector<Node>& nodes, int node, const int64_t* pc, const int* g)
+{
+    while (nodes[node].left >= 0) {
+        const int a = axis_of_h(nodes[node].h);
+        const Node& lc = nodes[nodes[node].left];
+        node = prefix_bits(pc[a], g[a], lc.len[a]) == lc.code[a] ? nodes[node].left : nodes[node].right;
+    }
+    return node;
+}
+
+btc_status blocking(const int32_t* xyz, int64_t n, int I, int J, int K, int bs, int threads, Schedule& s)
 {
     Axis ax[3];
     ax[0].init(I);
@@ -127,18 +139,57 @@ btc_status blocking(const int32_t* xyz, int64_t n, int I, int J, int K, int bs, 
     t1.reserve(bs + 1);
     t2.reserve(bs + 1);
 
-    for (int64_t i = 0; i < n; i++) {
+    // Entries are routed in chunks on several threads against a snapshot of
+    // the tree and of the global levels, then inserted in order.  Internal
+    // nodes never change once split, so an entry whose snapshot leaf is still
+    // a leaf has the route the reference would compute now; a leaf that split
+    // since the snapshot is descended further, and a change of a global level
+    // (which changes every bucket code) re-routes from the root.
+    const int64_t CH = 1 << 16;
+    std::vector<int> leaf((size_t)std::min<int64_t>(n, CH));
+    std::vector<int64_t> codes((size_t)std::min<int64_t>(n, CH) * 3);
+    std::atomic<int> bad(0);
+    for (int64_t base = 0; base < n; base += CH) {
+        const int64_t cn = std::min<int64_t>(CH, n - base);
+        const int g0[3] = {g[0], g[1], g[2]};
+        {
+            auto work = [&](int64_t lo, int64_t hi) {
+                for (int64_t k = lo; k < hi; k++) {
+                    const int32_t* p = xyz + 3 * (base + k);
+                    int64_t* pc = &codes[(size_t)(3 * k)];
+                    for (int a = 0; a < 3; a++)
+                        if (!ax[a].hx(g0[a], p[a], pc[a])) {
+                            bad = 1;
+                            return;
+                        }
+                    leaf[(size_t)k] = route(nodes, 0, pc, g0);
+                }
+            };
+            const int nt = std::max(1, std::min<int>(threads, (int)(cn / 4096) + 1));
+            std::vector<std::thread> pool;
+            for (int t = 1; t < nt; t++)
+                pool.emplace_back(work, cn * t / nt, cn * (t + 1) / nt);
+            work(0, cn / nt);
+            for (auto& t : pool)
+                t.join();
+            if (bad)
+                return BTC_ERR_RANGE;
+        }
+      for (int64_t k = 0; k < cn; k++) {
+        const int64_t i = base + k;
         const int32_t* p = xyz + 3 * i;
         int64_t pc[3];
-        for (int a = 0; a < 3; a++)
-            if (!ax[a].hx(g[a], p[a], pc[a]))
-                return BTC_ERR_RANGE;
-        int node = 0;
-        while (nodes[node].left >= 0) {
-            int a = axis_of_h(nodes[node].h);
-            const Node& lc = nodes[nodes[node].left];
-            node = prefix_bits(pc[a], g[a], lc.len[a]) == lc.code[a] ? nodes[node].left
-                                                                    : nodes[node].right;
+        int node;
+        if (g[0] == g0[0] && g[1] == g0[1] && g[2] == g0[2]) {
+            pc[0] = codes[(size_t)(3 * k)];
+            pc[1] = codes[(size_t)(3 * k + 1)];
+            pc[2] = codes[(size_t)(3 * k + 2)];
+            node = route(nodes, leaf[(size_t)k], pc, g);
+        } else {
+            for (int a = 0; a < 3; a++)
+                if (!ax[a].hx(g[a], p[a], pc[a]))
+                    return BTC_ERR_RANGE;
+            node = route(nodes, 0, pc, g);
         }
         int id = nodes[node].block;
         if ((int)blocks[id].ent.size() < bs) {
@@ -225,6 +276,7 @@ btc_status blocking(const int32_t* xyz, int64_t n, int I, int J, int K, int bs, 
             if ((int)NB.ent.capacity() < bs)
                 NB.ent.reserve(bs);
         }
+      }
     }
     for (auto& b : blocks)
         finish_block_codes(b);
@@ -459,7 +511,7 @@ btc_status build_schedule(const btc_config& cfg, const int32_t* xyz, int64_t n, 
     s.pss = cfg.parallel_sequence_size;
     s.train_nnz = n;
     double t0 = now_s();
-    btc_status rc = blocking(xyz, n, cfg.I, cfg.J, cfg.K, cfg.block_s, s);
+    btc_status rc = blocking(xyz, n, cfg.I, cfg.J, cfg.K, cfg.block_s, threads, s);
     if (rc != BTC_OK)
         return rc;
     double t1 = now_s();
