@@ -50,6 +50,10 @@ WORKLOADS = {
                train=0.9, R=16, lr=0.01, reg=0.01, epochs=10,
                desc="plain small: I=J=K=1000, 1M nnz uniform, rank-8 GT + N(0,0.01), 90/10 split, R=16, "
                     "lr 0.01, lambda 0.01"),
+    "c3": dict(I=200000, J=2000, K=1000000, nnz=200_000_000, zipf=(1.5, 0.0, 1.5), gt_rank=0, noise=0.0,
+               train=0.9, R=64, lr=0.01, reg=0.01, epochs=30,
+               desc="heavily skewed large: I=200k J=2k K=1M, 200M nnz, Zipf(1.5) on modes 1 and 3, uniform mode 2, "
+                    "log-normal(0,1) values rescaled to [0,1], 90/10 split, R=64, lr 0.01, lambda 0.01"),
     "small": dict(I=20000, J=20000, K=5000, nnz=2_000_000, zipf=(1.2, 1.2, 1.2), gt_rank=16, noise=0.05,
                   train=0.9, R=32, lr=0.005, reg=0.02, epochs=10,
                   desc="small skewed: I=J=20k K=5k, 2M nnz Zipf(1.2), R=32"),

@@ -288,19 +288,34 @@ btc_status blocking(const int32_t* xyz, int64_t n, int I, int J, int K, int bs, 
 // search_parallel_block_Tree as first-fit in ascending block id.
 void strata_first_fit(Schedule& s)
 {
+    // A stratum's members are pairwise disjoint on every axis, so the measure
+    // of an axis they cover is the sum of their dyadic interval lengths
+    // (axis = 2^63 units, a level-L id covers 2^(64-L)).  A block needs at
+    // least its own length free on each axis, and a stratum that covers a
+    // whole axis can never take another block: both only skip strata the
+    // exact test would reject, so the first fit is unchanged.
+    const uint64_t FULL = 1ULL << 63;
     struct St {
         uint64_t bins[3] = {0, 0, 0};
+        uint64_t used[3] = {0, 0, 0};
         std::vector<int32_t> mem;
     };
     std::vector<St> st;
+    std::vector<int32_t> open;  // strata that can still take a block, in creation order
+    size_t closed_since = 0;
     const auto& B = s.blocks;
     for (int32_t b = 0; b < (int32_t)B.size(); b++) {
         if (B[b].ent.empty())
             continue;
         const BlockRec& cb = B[b];
-        size_t k = 0;
-        for (; k < st.size(); k++) {
-            St& S = st[k];
+        uint64_t len[3];
+        for (int a = 0; a < 3; a++)
+            len[a] = 1ULL << (64 - cb.level[a]);
+        int32_t found = -1;
+        for (int32_t k : open) {
+            St& S = st[(size_t)k];
+            if (FULL - S.used[0] < len[0] || FULL - S.used[1] < len[1] || FULL - S.used[2] < len[2])
+                continue;
             bool ok = true;
             for (int a = 0; a < 3 && ok; a++) {
                 if ((S.bins[a] & cb.bins[a]) == 0)
@@ -311,15 +326,33 @@ void strata_first_fit(Schedule& s)
                         break;
                     }
             }
-            if (ok)
+            if (ok) {
+                found = k;
                 break;
+            }
         }
-        if (k == st.size())
+        if (found < 0) {
+            found = (int32_t)st.size();
             st.emplace_back();
-        St& S = st[k];
+            open.push_back(found);
+        }
+        St& S = st[(size_t)found];
         S.mem.push_back(b);
-        for (int a = 0; a < 3; a++)
+        bool full = false;
+        for (int a = 0; a < 3; a++) {
             S.bins[a] |= cb.bins[a];
+            S.used[a] += len[a];
+            full |= S.used[a] >= FULL;
+        }
+        if (full && ++closed_since >= 64) {
+            open.erase(std::remove_if(open.begin(), open.end(),
+                                      [&](int32_t k) {
+                                          const St& T = st[(size_t)k];
+                                          return T.used[0] >= FULL || T.used[1] >= FULL || T.used[2] >= FULL;
+                                      }),
+                       open.end());
+            closed_since = 0;
+        }
     }
     s.strata_off.assign(1, 0);
     s.strata_ids.clear();
