@@ -325,9 +325,18 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
                             float* mm = m == 0 ? a.master[0] : (m == 1 ? a.master[1] : a.master[2]);
                             red_v(mm + (size_t)hm * Rp + o, d);
                         } else {
+                            // fresh random bits for every rounding: a row without a
+                            // master is written at most once per tile visit, and a
+                            // block padded into several slots visits its tiles once
+                            // per slot, so (epoch seed, mode, slot, tile, row,
+                            // column) names one update.  Bits reused across the
+                            // updates of an epoch would round an element the same
+                            // way every time and let its magnitude drift by up to
+                            // one ulp per update.
                             unsigned* wp = reinterpret_cast<unsigned*>(Fm + (size_t)g * Rp + o);
-                            const unsigned rnd0 = mix3(seed ^ (unsigned)(m * 0x68E31DA4u), (unsigned)g, (unsigned)o);
-                            const unsigned rnd1 = mix3(seed ^ (unsigned)(m * 0x68E31DA4u), (unsigned)g, (unsigned)o + 2);
+                            const unsigned ts = mix3(seed ^ (unsigned)(m * 0x68E31DA4u), (unsigned)t, (unsigned)slot);
+                            const unsigned rnd0 = mix3(ts, (unsigned)g, (unsigned)o);
+                            const unsigned rnd1 = mix3(ts, (unsigned)g, (unsigned)o + 2);
                             bool ok = true;
                             if (d.x != 0.f || d.y != 0.f)
                                 ok &= add_pair_sr(wp, d.x, d.y, rnd0);

@@ -174,3 +174,39 @@ def test_bf16_stochastic_rounding_is_unbiased():
     ulp = 0.0625 * 2.0 ** -7
     assert 0 < d32.mean() < 0.5 * ulp  # the whole epoch moves a row by less than one ulp ...
     assert abs(d16.mean() - d32.mean()) <= 0.05 * d32.mean()  # ... and the BF16 rows move as much on average
+
+
+def test_bf16_stochastic_rounding_per_element():
+    """Every stochastic rounding draws fresh random bits, so each element's
+    BF16 change follows its own FP32 change, not only the mean over elements.
+
+    A uniform 500^3 tensor of 250k entries gives every row ~500 entries per
+    epoch spread over many tiles, and padding runs some blocks in several
+    slots.  Each element takes many sub-ulp increments (about 1.1 ulp in
+    total).  Independent roundings leave it a Poisson-like number of ulps
+    from the FP32 result: RMS about 1 ulp, and above 10 ulp with probability
+    below 1e-3 over all 24k elements.  Bits shared across the updates of an
+    epoch (one draw per element, or one per tile for a block visited from
+    several slots) round an element the same way every time; on this tensor
+    that put elements 20-40 ulp away."""
+    n, R = 500, 16
+    tx, _, _, _ = bg.gen_tensor(n, n, n, 250_000, gt_rank=4, train_frac=1.0, seed=7)
+    val = np.ones(len(tx))  # every update pushes the same way
+    cfg = dict(I=n, J=n, K=n, rank=R, lr=2e-4, reg=0.0, mode=bg.STAGED, resident_blocks=-1)
+    s = bg.Schedule(bg.config(**cfg), tx)
+    base = [np.full((n, R), 0.0625) for _ in range(3)]  # exactly representable in BF16
+    ulp = 0.0625 * 2.0 ** -7
+    out = {}
+    for dt in (bg.F32, bg.BF16):
+        ctx = bg.Context(bg.config(dtype=dt, **cfg), s, tx, val, tx, val)
+        for m in range(3):
+            ctx.set_factors(m, base[m])
+        assert ctx.train_epoch().device_status == 0
+        out[dt] = np.stack([ctx.get_factors(m) - base[m] for m in range(3)]) / ulp
+        ctx.close()
+    d32, d16 = out[bg.F32], out[bg.BF16]
+    assert 0.5 < d32.mean() < 2.0 and d32.max() < 4.0  # many sub-ulp increments, about one ulp in all
+    err = d16 - d32
+    assert abs(d16.mean() - d32.mean()) <= 0.05 * d32.mean()
+    assert np.sqrt((err ** 2).mean()) <= 1.6, np.sqrt((err ** 2).mean())
+    assert np.abs(err).max() <= 10.0, np.abs(err).max()
