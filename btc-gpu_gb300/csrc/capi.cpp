@@ -67,7 +67,7 @@ struct btc_ctx {
     int* slot_ntiles = nullptr;
     int4* tent = nullptr;
     unsigned short* tcsr = nullptr;
-    int4* tsegs = nullptr;
+    unsigned* tsegs = nullptr;
     int* trows = nullptr;
     double* tval64 = nullptr;
     int* counter = nullptr;
@@ -75,7 +75,6 @@ struct btc_ctx {
     int nunits = 0;
     // BF16 storage: FP32 masters of the hottest rows
     float* master[3] = {nullptr, nullptr, nullptr};
-    int* hot_map[3] = {nullptr, nullptr, nullptr};
     int* hot_rows[3] = {nullptr, nullptr, nullptr};
     int nhot[3] = {0, 0, 0};
     unsigned epoch = 0;
@@ -353,7 +352,6 @@ btc_status btc_ctx_destroy(btc_ctx* c)
     free_dev(c->tile_ns);
     for (int a = 0; a < 3; a++) {
         free_dev(c->master[a]);
-        free_dev(c->hot_map[a]);
         free_dev(c->hot_rows[a]);
     }
     if (c->ev0)
@@ -548,13 +546,27 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
             return rc;
         if ((rc = upload((void**)&c->tcsr, ts.csr.data(), ts.csr.size() * 2, c->stream)))
             return rc;
-        if ((rc = upload((void**)&c->tsegs, ts.segs.data(), ts.segs.size() * sizeof(int4), c->stream)))
-            return rc;
-        if ((rc = upload((void**)&c->trows, ts.rows.data(), ts.rows.size() * 4, c->stream)))
-            return rc;
+        {
+            // owner segments packed into one word each, as the kernel reads
+            // them: local row (14 bits; cap <= 16383), mode (2), count - 1
+            // (4; segments hold <= 16 entries), start in the mode's CSR list
+            // (12; a tile holds <= 4096 entries)
+            std::vector<uint32_t> seg32(ts.segs.size());
+            for (size_t q = 0; q < ts.segs.size(); q++) {
+                const int4& g = ts.segs[q];
+                if (g.x < 0 || g.x >= (1 << 14) || g.y < 0 || g.y > 2 || g.w < 1 || g.w > 16 || g.z < 0 ||
+                    g.z >= (1 << 12))
+                    return BTC_ERR_UNSUPPORTED;
+                seg32[q] = (uint32_t)g.x | ((uint32_t)g.y << 14) | ((uint32_t)(g.w - 1) << 16) |
+                           ((uint32_t)g.z << 20);
+            }
+            if ((rc = upload((void**)&c->tsegs, seg32.data(), seg32.size() * 4, c->stream)))
+                return rc;
+        }
         if (!ts.val64.empty() && (rc = upload((void**)&c->tval64, ts.val64.data(), ts.val64.size() * 8, c->stream)))
             return rc;
         if (c->dtype == BTC_DTYPE_BF16) {
+            std::vector<int> maps[3];
             // FP32 masters for the rows whose BF16 copy would be contended:
             // every row that a tile updates through more than one owner
             // segment (those segments add to it concurrently) and every row
@@ -592,15 +604,26 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
                 for (size_t h = 0; h < hot.size(); h++)
                     map[(size_t)hot[h]] = (int)h;
                 c->nhot[a] = (int)hot.size();
-                if ((rc = upload((void**)&c->hot_map[a], map.data(), map.size() * 4, c->stream)))
-                    return rc;
                 if ((rc = upload((void**)&c->hot_rows[a], hot.data(), hot.size() * 4, c->stream)))
                     return rc;
                 const size_t mb = std::max<size_t>(16, hot.size() * c->Rp * sizeof(float));
                 CK(cudaMalloc((void**)&c->master[a], mb));
                 CK(cudaMemsetAsync(c->master[a], 0, mb, c->stream));
+                maps[a].swap(map);
             }
+            // the kernel finds a row's master in its staged row id: ~(master
+            // index) instead of the global row, so staging needs no lookup
+            for (const btc::TileHdr& h : ts.tiles)
+                for (int r = 0; r < h.nrows; r++) {
+                    const int m = r < h.nx ? 0 : (r < h.nx + h.ny ? 1 : 2);
+                    int32_t& g = ts.rows[(size_t)(h.roff + r)];
+                    const int hm = maps[m][(size_t)g];
+                    if (hm >= 0)
+                        g = ~hm;
+                }
         }
+        if ((rc = upload((void**)&c->trows, ts.rows.data(), ts.rows.size() * 4, c->stream)))
+            return rc;
         CK(cudaMalloc((void**)&c->counter, sizeof(int)));
         {
             std::vector<int> uo((size_t)nslots + 1);
@@ -787,10 +810,8 @@ static btc::StagedArgs staged_args(btc_ctx* c)
     s.G = c->st_G;
     s.NV = c->st_NV;
     s.status = c->status;
-    for (int a = 0; a < 3; a++) {
+    for (int a = 0; a < 3; a++)
         s.master[a] = c->master[a];
-        s.hot[a] = c->hot_map[a];
-    }
     return s;
 }
 

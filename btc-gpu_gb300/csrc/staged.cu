@@ -10,8 +10,10 @@
 //   3. owners  one lane group per owner segment (a run of <= seg entries
 //              sharing a row of one mode) sums err * (other two rows) from S
 //              in registers and adds coe*lr*(sum - count*reg*row) to the row
-//              in global memory with one vector atomic per 16 bytes, so a row
-//              is written once per segment instead of once per entry.
+//              in global memory with one vector atomic per 16 bytes (BF16
+//              rows without a master: one stochastically rounding 8-byte
+//              compare-and-swap per 4 elements), so a row is written once per
+//              segment instead of once per entry.
 // Inside a tile the update is the reference kernel's: all entries of one
 // thread_size wave read rows before their deltas land (sgd_Kernel.cu:358-392),
 // coe-weighted, L2-regularised per visit.  Tiles of one slot run in order on
@@ -89,16 +91,24 @@ __device__ __forceinline__ float4 bf16x4_to_float4(uint2 raw)
     return make_float4(__uint_as_float(raw.x << 16), __uint_as_float(raw.x & 0xffff0000u),
                        __uint_as_float(raw.y << 16), __uint_as_float(raw.y & 0xffff0000u));
 }
-// Adds (d0, d1) to one BF16 pair with stochastic rounding, by compare-and-
-// swap; gives up (returns false) after a bounded number of attempts.
-__device__ __forceinline__ bool add_pair_sr(unsigned* w, float d0, float d1, unsigned rnd)
+// Adds d to four consecutive BF16 elements (8 bytes, 8-byte aligned) with
+// stochastic rounding, by one 64-bit compare-and-swap per attempt.  The first
+// attempt assumes the elements still hold `guess` (the tile's snapshot of
+// them), so an uncontended row costs one round trip to L2; a stale guess only
+// costs a retry from the value the swap returned.  Element k takes random
+// bits 16k..16k+15 of (r0, r1).  Gives up (returns false) after a bounded
+// number of attempts.
+__device__ __forceinline__ bool add_quad_sr(unsigned long long* w, float4 d, unsigned r0, unsigned r1, uint2 guess)
 {
-    unsigned old = __ldcg(w);
+    unsigned long long old = ((unsigned long long)guess.y << 32) | guess.x;
     for (int it = 0; it < (1 << 16); it++) {
-        const float lo = __uint_as_float(old << 16) + d0;
-        const float hi = __uint_as_float(old & 0xffff0000u) + d1;
-        const unsigned nw = sr_bf16_bits(lo, rnd) | (sr_bf16_bits(hi, rnd >> 16) << 16);
-        const unsigned prev = atomicCAS(w, old, nw);
+        const unsigned lo = (unsigned)old, hi = (unsigned)(old >> 32);
+        const unsigned nlo = sr_bf16_bits(__uint_as_float(lo << 16) + d.x, r0) |
+                             (sr_bf16_bits(__uint_as_float(lo & 0xffff0000u) + d.y, r0 >> 16) << 16);
+        const unsigned nhi = sr_bf16_bits(__uint_as_float(hi << 16) + d.z, r1) |
+                             (sr_bf16_bits(__uint_as_float(hi & 0xffff0000u) + d.w, r1 >> 16) << 16);
+        const unsigned long long nw = ((unsigned long long)nhi << 32) | nlo;
+        const unsigned long long prev = atomicCAS(w, old, nw);
         if (prev == old)
             return true;
         old = prev;
@@ -110,6 +120,13 @@ __device__ __forceinline__ float4 ld_bf4(const unsigned short* p)
 {
     return bf16x4_to_float4(*reinterpret_cast<const uint2*>(p));
 }
+
+// Owner segment packed in one word: local row (bits 0-13), mode (14-15),
+// count - 1 (16-19), start in that mode's CSR list (20-31).
+__device__ __forceinline__ int seg_row(unsigned s) { return (int)(s & 0x3fffu); }
+__device__ __forceinline__ int seg_mode(unsigned s) { return (int)((s >> 14) & 3u); }
+__device__ __forceinline__ int seg_count(unsigned s) { return (int)((s >> 16) & 15u) + 1; }
+__device__ __forceinline__ int seg_start(unsigned s) { return (int)(s >> 20); }
 __device__ __forceinline__ unsigned pack_bf16x2_rn(float lo, float hi)
 {
     return (unsigned)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
@@ -167,6 +184,12 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
             const TileHdr h = a.tiles[t];
             const int nv = h.nrows * vpr;
             const int nxy = h.nx + h.ny;
+            // the first owner segment of this lane group, fetched now so that
+            // its latency hides behind staging and the errors
+            const int seg_stride = nwarps * EPW;
+            unsigned sg_next = 0;
+            if (warp * EPW + sub < h.nseg)
+                sg_next = __ldg(&a.segs[h.soff + warp * EPW + sub]);
             // 1. stage: rows, entries and CSR lists, all as 16-byte async copies
             //    (BF16 rows are widened to FP32 through registers)
             if constexpr (BF) {
@@ -175,18 +198,16 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
                 unsigned short* Sb = reinterpret_cast<unsigned short*>(smem);
                 for (int i = tid; i < nc; i += blockDim.x) {
                     const int r = i / cpr, c = i - r * cpr;
+                    // the global row, or ~(master index) for a row with an FP32 master
                     const int g = __ldg(&a.rows[h.roff + r]);
                     const int m = r < h.nx ? 0 : (r < nxy ? 1 : 2);
-                    const int* hotm = m == 0 ? a.hot[0] : (m == 1 ? a.hot[1] : a.hot[2]);
-                    const int hm = __ldg(&hotm[g]);
-                    if (c == 0) {
+                    if (c == 0)
                         rid[r] = g;
-                        rid[a.cap + r] = hm;
-                    }
-                    if (hm >= 0) {
+                    if (g < 0) {
                         const float* mm = m == 0 ? a.master[0] : (m == 1 ? a.master[1] : a.master[2]);
-                        const float4 v0 = __ldcg(reinterpret_cast<const float4*>(mm + (size_t)hm * Rp + c * 8));
-                        const float4 v1 = __ldcg(reinterpret_cast<const float4*>(mm + (size_t)hm * Rp + c * 8 + 4));
+                        const size_t hm = (size_t)(~g);
+                        const float4 v0 = __ldcg(reinterpret_cast<const float4*>(mm + hm * Rp + c * 8));
+                        const float4 v1 = __ldcg(reinterpret_cast<const float4*>(mm + hm * Rp + c * 8 + 4));
                         uint4 q;
                         q.x = pack_bf16x2_rn(v0.x, v0.y);
                         q.y = pack_bf16x2_rn(v0.z, v0.w);
@@ -264,13 +285,16 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
             }
             __syncthreads();
             // 3. owner segments: reduce in registers, one vector add per 16 bytes
-            for (int s0 = warp * EPW; s0 < h.nseg; s0 += nwarps * EPW) {
+            //    (BF16: one 8-byte compare-and-swap per 4 elements)
+            for (int s0 = warp * EPW; s0 < h.nseg; s0 += seg_stride) {
                 const int s = s0 + sub;
+                const unsigned sg = sg_next;
+                if (s + seg_stride < h.nseg)
+                    sg_next = __ldg(&a.segs[h.soff + s + seg_stride]);
                 if (s >= h.nseg)
                     continue;
-                const int4 sg = __ldg(&a.segs[h.soff + s]);
-                const int row = sg.x, m = sg.y, cnt = sg.w;
-                const unsigned short* lst = csr + m * h.n + sg.z;
+                const int row = seg_row(sg), m = seg_mode(sg), cnt = seg_count(sg);
+                const unsigned short* lst = csr + m * h.n + seg_start(sg);
                 T acc[E];
 #pragma unroll
                 for (int i = 0; i < E; i++)
@@ -308,23 +332,25 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
                 const T w = m == 0 ? cx : (m == 1 ? cy : cz);
                 const T creg = (T)cnt * reg;
                 if constexpr (BF) {
-                    const int g = rid[row], hm = rid[a.cap + row];
+                    const int g = rid[row];  // global row, or ~(master index)
                     unsigned short* Fm = static_cast<unsigned short*>(m == 0 ? a.A : (m == 1 ? a.B : a.C));
 #pragma unroll
                     for (int j = 0; j < NV; j++) {
                         const int o = (j * G + gl) * VN;
                         if (MASK && o >= Rp)
                             continue;
-                        const float4 own = ld_bf4(reinterpret_cast<const unsigned short*>(smem) + (size_t)row * Rp + o);
+                        const uint2 raw = *reinterpret_cast<const uint2*>(
+                            reinterpret_cast<const unsigned short*>(smem) + (size_t)row * Rp + o);
+                        const float4 own = bf16x4_to_float4(raw);
                         float4 d;
                         d.x = w * (acc[j * VN + 0] - creg * own.x);
                         d.y = w * (acc[j * VN + 1] - creg * own.y);
                         d.z = w * (acc[j * VN + 2] - creg * own.z);
                         d.w = w * (acc[j * VN + 3] - creg * own.w);
-                        if (hm >= 0) {
+                        if (g < 0) {
                             float* mm = m == 0 ? a.master[0] : (m == 1 ? a.master[1] : a.master[2]);
-                            red_v(mm + (size_t)hm * Rp + o, d);
-                        } else {
+                            red_v(mm + (size_t)(~g) * Rp + o, d);
+                        } else if (d.x != 0.f || d.y != 0.f || d.z != 0.f || d.w != 0.f) {
                             // fresh random bits for every rounding: a row without a
                             // master is written at most once per tile visit, and a
                             // block padded into several slots visits its tiles once
@@ -333,16 +359,13 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
                             // updates of an epoch would round an element the same
                             // way every time and let its magnitude drift by up to
                             // one ulp per update.
-                            unsigned* wp = reinterpret_cast<unsigned*>(Fm + (size_t)g * Rp + o);
+                            // The four elements are 8-byte aligned: rows start on
+                            // 16 bytes (Rp is a multiple of 8) and o is a multiple of 4.
+                            auto* wp = reinterpret_cast<unsigned long long*>(Fm + (size_t)g * Rp + o);
                             const unsigned ts = mix3(seed ^ (unsigned)(m * 0x68E31DA4u), (unsigned)t, (unsigned)slot);
                             const unsigned rnd0 = mix3(ts, (unsigned)g, (unsigned)o);
                             const unsigned rnd1 = mix3(ts, (unsigned)g, (unsigned)o + 2);
-                            bool ok = true;
-                            if (d.x != 0.f || d.y != 0.f)
-                                ok &= add_pair_sr(wp, d.x, d.y, rnd0);
-                            if (d.z != 0.f || d.w != 0.f)
-                                ok &= add_pair_sr(wp + 1, d.z, d.w, rnd1);
-                            if (!ok)
+                            if (!add_quad_sr(wp, d, rnd0, rnd1, raw))
                                 atomicExch(a.status, 1);
                         }
                     }
@@ -462,7 +485,7 @@ int staged_cap_for(int dtype, int Rp, int wave, int ctas_per_sm, size_t smem_per
 {
     size_t es = dtype == 1 ? 8 : (dtype == 2 ? 2 : 4);
     size_t budget = std::min(smem_per_block, smem_per_sm / (size_t)std::max(1, ctas_per_sm) - 1024);
-    int cap = (int)std::min<size_t>(65535, budget / ((size_t)Rp * es + 8));
+    int cap = (int)std::min<size_t>(16383, budget / ((size_t)Rp * es + 4));
     while (cap > 0 && staged_smem_bytes(dtype, Rp, cap, wave) > budget)
         cap--;
     return cap;

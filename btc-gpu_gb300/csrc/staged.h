@@ -17,8 +17,10 @@ struct StagedArgs {
     int nunits;
     const int4* ent;
     const unsigned short* csr;
-    const int4* segs;
-    const int* rows;
+    const unsigned* segs;    // owner segments, one packed word each (row 14 bits, mode 2,
+                             // count - 1 4, start in the mode's CSR list 12)
+    const int* rows;         // global row of every staged row; BF16: ~(master index)
+                             // for a row with an FP32 master
     const double* val64;     // FP64 values (f64), else null
     void* A;
     void* B;
@@ -30,7 +32,6 @@ struct StagedArgs {
     int* counter;            // next slot to take (zeroed before each launch)
     // BF16 storage only
     float* master[3];        // FP32 master rows of the hottest rows of each mode
-    const int* hot[3];       // row -> master index, -1 when the row has none
     unsigned seed;           // stochastic-rounding stream of this epoch
     int* status;             // set to 1 when a rounding compare-and-swap gives up
     unsigned* tile_ns;       // when set: nanoseconds each tile took (globaltimer)
@@ -38,8 +39,7 @@ struct StagedArgs {
     const unsigned* seed_ptr;  // when set, the rounding stream is seed ^ *seed_ptr (graph replays)
 };
 
-// Shared-memory layout of one CTA: S rows | entries | errors | row ids and
-// master slots | CSR.
+// Shared-memory layout of one CTA: S rows | entries | errors | row ids | CSR.
 // Every region that receives 16-byte copies starts on a 16-byte boundary.
 // es = bytes of one staged row element (8 FP64, 4 FP32, 2 BF16); errors are
 // kept in the compute type (8 for FP64, else 4).
@@ -52,14 +52,15 @@ struct StagedLayout {
         ent = al((size_t)cap * Rp * es);
         err = al(ent + (size_t)wave * 16);
         rid = al(err + (size_t)wave * ee);
-        csr = al(rid + (size_t)cap * 8);
+        csr = al(rid + (size_t)cap * 4);
         total = al(csr + (3 * (size_t)wave + 8) * 2);
     }
 };
 
 // Shared-memory bytes of one CTA for a dtype, rank stride, cap and wave.
 size_t staged_smem_bytes(int dtype, int Rp, int cap, int wave);
-// Largest cap that fits `ctas_per_sm` CTAs on one SM.
+// Largest cap that fits `ctas_per_sm` CTAs on one SM (at most 16383: a
+// segment word holds the local row in 14 bits).
 int staged_cap_for(int dtype, int Rp, int wave, int ctas_per_sm, size_t smem_per_sm, size_t smem_per_block);
 cudaError_t launch_staged(int dtype, const StagedArgs& a, int grid, int block, cudaStream_t st);
 // Many tensors in one launch: `tensors` (device) holds each tensor's
