@@ -54,6 +54,10 @@ WORKLOADS = {
                train=0.9, R=64, lr=0.01, reg=0.01, epochs=30,
                desc="heavily skewed large: I=200k J=2k K=1M, 200M nnz, Zipf(1.5) on modes 1 and 3, uniform mode 2, "
                     "log-normal(0,1) values rescaled to [0,1], 90/10 split, R=64, lr 0.01, lambda 0.01"),
+    "c5": dict(I=1_000_000, J=1_000_000, K=100_000, nnz=1_000_000_000, zipf=(1.3, 1.3, 1.3), gt_rank=32,
+               noise=0.05, train=0.95, R=32, lr=0.005, reg=0.02, epochs=10,
+               desc="largest single tensor: I=J=1M K=100k, 1B nnz Zipf(1.3) per mode, rank-32 GT + N(0,0.05), "
+                    "95/5 split, R=32, lr 0.005, lambda 0.02"),
     "small": dict(I=20000, J=20000, K=5000, nnz=2_000_000, zipf=(1.2, 1.2, 1.2), gt_rank=16, noise=0.05,
                   train=0.9, R=32, lr=0.005, reg=0.02, epochs=10,
                   desc="small skewed: I=J=20k K=5k, 2M nnz Zipf(1.2), R=32"),
@@ -150,11 +154,13 @@ def cfg_for(w, dtype, mode, device=0):
                      parallel_sequence_size=8, dtype=dtype, mode=mode, device=device, ctas_per_sm=CTAS)
 
 
-def flat_schedule(sched):
+def flat_schedule(sched, max_updates=250_000_000):
+    """The leading strata of the schedule as flat arrays for the CPU replays
+    (every CPU sample stays well inside 250M updates)."""
     import oracle
 
     off, ids, coe = sched.groups()
-    return oracle.FlatSchedule(off, ids, coe, sched.block_entries)
+    return oracle.FlatSchedule(off, ids, coe, sched.block_entries, max_updates=max_updates)
 
 
 def init_factors(w):
@@ -203,7 +209,7 @@ def run_reference(args):
         times.append(t)
     value = sum(ups) / sum(times)
     sample = ("first %d of %d strata of one epoch per step (%.0f updates/step), FP64 Hogwild threads, "
-              "schedule identical to the reference's block_problem" % (g, flat.ngroups, np.mean(ups)))
+              "schedule identical to the reference's block_problem" % (g, sched.summary.num_groups, np.mean(ups)))
     line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "updates/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * np.mean(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -369,7 +375,7 @@ def run_gpu(args):
         u, tcpu, g = cpu_sample(flat, tx, tv, w, args.cpu_seconds, 1)
         cpu = {"value": u / tcpu, "unit": "updates/s", "cores": 1, "kind": "port",
                "sample": "first %d of %d strata of one epoch (%d updates), serial FP64 replay of the "
-                         "reference update rule" % (g, flat.ngroups, u)}
+                         "reference update rule" % (g, sm.num_groups, u)}
         line = {"metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",

@@ -162,22 +162,33 @@ class FlatSchedule:
     """A schedule given as flat arrays (groups -> slots -> entry indices), for
     replaying the reference update rule on host cores (the CPU baseline)."""
 
-    def __init__(self, group_off, slot_blocks, slot_coe, block_entries):
-        self.goff = np.ascontiguousarray(group_off, np.int64)
-        sizes = np.array([len(block_entries(int(b))) for b in slot_blocks], np.int64)
-        self.soff = np.zeros(len(slot_blocks) + 1, np.int64)
-        np.cumsum(sizes, out=self.soff[1:])
+    def __init__(self, group_off, slot_blocks, slot_coe, block_entries, max_updates=None):
+        """max_updates: keep only the leading groups, up to the first group
+        boundary at or past this many updates (a bounded sample of a large
+        schedule); None keeps them all."""
+        goff = np.asarray(group_off, np.int64)
         cache = {}
         parts = []
-        for b in slot_blocks:
-            b = int(b)
-            if b not in cache:
-                cache[b] = np.asarray(block_entries(b), np.int32)
-            parts.append(cache[b])
-        self.ent = np.ascontiguousarray(np.concatenate(parts) if parts else np.zeros(0, np.int32))
-        self.coe = np.ascontiguousarray(slot_coe, np.float64)
-        self.nslots = len(slot_blocks)
-        self.ngroups = len(self.goff) - 1
+        total = 0
+        ngroups = len(goff) - 1
+        for g in range(ngroups):
+            if max_updates is not None and total >= max_updates:
+                ngroups = g
+                break
+            for k in range(int(goff[g]), int(goff[g + 1])):
+                b = int(slot_blocks[k])
+                if b not in cache:
+                    cache[b] = np.asarray(block_entries(b), np.int32)
+                parts.append(cache[b])
+                total += len(cache[b])
+        self.goff = np.ascontiguousarray(goff[: ngroups + 1])
+        nslots = int(self.goff[-1]) if ngroups > 0 else 0
+        self.soff = np.zeros(nslots + 1, np.int64)
+        np.cumsum([len(p) for p in parts[:nslots]], out=self.soff[1:])
+        self.ent = np.ascontiguousarray(np.concatenate(parts[:nslots]) if nslots else np.zeros(0, np.int32))
+        self.coe = np.ascontiguousarray(np.asarray(slot_coe, np.float64).reshape(-1)[: 3 * nslots])
+        self.nslots = nslots
+        self.ngroups = ngroups
 
     def replay(self, xyz, val, R, lr, reg, A, B, C, s0=0, s1=None):
         lib = _load()
