@@ -286,7 +286,7 @@ btc_status blocking(const int32_t* xyz, int64_t n, int I, int J, int K, int bs, 
 }
 
 // search_parallel_block_Tree as first-fit in ascending block id.
-void strata_first_fit(Schedule& s)
+void strata_first_fit(Schedule& s, int threads)
 {
     // A stratum's members are pairwise disjoint on every axis, so the measure
     // of an axis they cover is the sum of their dyadic interval lengths
@@ -304,6 +304,58 @@ void strata_first_fit(Schedule& s)
     std::vector<int32_t> open;  // strata that can still take a block, in creation order
     size_t closed_since = 0;
     const auto& B = s.blocks;
+    auto fits = [&](const St& S, const BlockRec& cb, const uint64_t* len) {
+        if (FULL - S.used[0] < len[0] || FULL - S.used[1] < len[1] || FULL - S.used[2] < len[2])
+            return false;
+        for (int a = 0; a < 3; a++) {
+            if ((S.bins[a] & cb.bins[a]) == 0)
+                continue;
+            for (int32_t m : S.mem)
+                if (axis_conflict(B[m], cb, a))
+                    return false;
+        }
+        return true;
+    };
+    // The scan over the open strata for one block is read-only, so long
+    // scans are split into contiguous shares of the open list, one per
+    // thread; a share stops at its first fit or once a lower share has found
+    // one, and the lowest position found is the first fit.
+    const int T = std::max(1, std::min(threads, 64));
+    const size_t PAR_MIN = 4096;
+    std::atomic<int> gen(0), done(0);
+    std::atomic<bool> quit(false);
+    std::atomic<int64_t> best(INT64_MAX);
+    const BlockRec* cur = nullptr;
+    uint64_t cur_len[3] = {0, 0, 0};
+    size_t n_open = 0;
+    auto scan = [&](int t) {
+        const size_t lo = n_open * (size_t)t / (size_t)T, hi = n_open * (size_t)(t + 1) / (size_t)T;
+        for (size_t q = lo; q < hi; q++) {
+            if ((int64_t)q >= best.load(std::memory_order_relaxed))
+                return;
+            if (fits(st[(size_t)open[q]], *cur, cur_len)) {
+                int64_t b0 = best.load(std::memory_order_relaxed);
+                while ((int64_t)q < b0 && !best.compare_exchange_weak(b0, (int64_t)q, std::memory_order_relaxed))
+                    ;
+                return;
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < T; t++)
+        pool.emplace_back([&, t] {
+            int seen = 0;
+            for (;;) {
+                int g;
+                while ((g = gen.load(std::memory_order_acquire)) == seen)
+                    std::this_thread::yield();
+                seen = g;
+                if (quit.load(std::memory_order_acquire))
+                    return;
+                scan(t);
+                done.fetch_add(1, std::memory_order_acq_rel);
+            }
+        });
     for (int32_t b = 0; b < (int32_t)B.size(); b++) {
         if (B[b].ent.empty())
             continue;
@@ -312,24 +364,26 @@ void strata_first_fit(Schedule& s)
         for (int a = 0; a < 3; a++)
             len[a] = 1ULL << (64 - cb.level[a]);
         int32_t found = -1;
-        for (int32_t k : open) {
-            St& S = st[(size_t)k];
-            if (FULL - S.used[0] < len[0] || FULL - S.used[1] < len[1] || FULL - S.used[2] < len[2])
-                continue;
-            bool ok = true;
-            for (int a = 0; a < 3 && ok; a++) {
-                if ((S.bins[a] & cb.bins[a]) == 0)
-                    continue;
-                for (int32_t m : S.mem)
-                    if (axis_conflict(B[m], cb, a)) {
-                        ok = false;
-                        break;
-                    }
-            }
-            if (ok) {
-                found = k;
-                break;
-            }
+        if (T > 1 && open.size() >= PAR_MIN) {
+            cur = &cb;
+            for (int a = 0; a < 3; a++)
+                cur_len[a] = len[a];
+            n_open = open.size();
+            best.store(INT64_MAX, std::memory_order_relaxed);
+            done.store(0, std::memory_order_relaxed);
+            gen.fetch_add(1, std::memory_order_acq_rel);
+            scan(0);
+            while (done.load(std::memory_order_acquire) < T - 1)
+                std::this_thread::yield();
+            const int64_t q = best.load(std::memory_order_relaxed);
+            if (q != INT64_MAX)
+                found = open[(size_t)q];
+        } else {
+            for (int32_t k : open)
+                if (fits(st[(size_t)k], cb, len)) {
+                    found = k;
+                    break;
+                }
         }
         if (found < 0) {
             found = (int32_t)st.size();
@@ -354,6 +408,10 @@ void strata_first_fit(Schedule& s)
             closed_since = 0;
         }
     }
+    quit.store(true, std::memory_order_release);
+    gen.fetch_add(1, std::memory_order_acq_rel);
+    for (auto& t : pool)
+        t.join();
     s.strata_off.assign(1, 0);
     s.strata_ids.clear();
     s.max_parallel_cf = 0;
@@ -548,7 +606,7 @@ btc_status build_schedule(const btc_config& cfg, const int32_t* xyz, int64_t n, 
     if (rc != BTC_OK)
         return rc;
     double t1 = now_s();
-    strata_first_fit(s);
+    strata_first_fit(s, threads);
     double t2 = now_s();
     s.target = stratum_target(s.max_parallel_cf, (int32_t)s.blocks.size(), s.pss, resident);
     balance(s, threads);

@@ -64,6 +64,46 @@ def test_groups_slots_coe_match_reference(built):
         assert [tuple(v) for v in xyz[ent].tolist()] == sl["xyz"]
 
 
+@pytest.mark.parametrize("seed,dims,nnz,zipf,block_s", [
+    (11, (3000, 3000, 3000), 200_000, (0.0, 0.0, 0.0), 256),
+    (12, (20000, 20000, 5000), 300_000, (1.2, 1.2, 1.2), 512),
+    (13, (50000, 500, 200000), 300_000, (1.5, 0.0, 1.5), 512),
+    (14, (100000, 100000, 10000), 400_000, (1.3, 1.3, 1.3), 2048),
+    (15, (2000, 2000, 2000), 100_000, (1.5, 1.5, 1.5), 64),
+])
+def test_strata_and_groups_match_oracle_on_skewed_inputs(seed, dims, nnz, zipf, block_s):
+    """The product builder (indexed first-fit strata, threaded padding) gives
+    the oracle's strata, groups and coe weights on larger skewed inputs than
+    the fixtures: hot rows make long chains of mutually conflicting blocks."""
+    import oracle
+
+    I, J, K = dims
+    tx, _, _, _ = bg.gen_tensor(I, J, K, nnz, zipf=zipf, train_frac=1.0, seed=seed)
+    o = oracle.Schedule(tx, I, J, K, block_s, 8)
+    s = bg.Schedule(bg.config(I=I, J=J, K=K, block_s=block_s, parallel_sequence_size=8, resident_blocks=-1), tx)
+    assert s.summary.num_strata == o.nstrata
+    assert s.strata() == o.strata
+    off, ids, coe = s.groups()
+    assert np.array_equal(off, o.group_off) and np.array_equal(ids, o.slot_ids)
+    assert np.array_equal(coe, o.slot_coe)
+
+
+def test_threaded_builder_equals_serial_builder():
+    """With thousands of open strata the first-fit scan is split over host
+    threads (and padding runs per group on threads); the schedule must not
+    depend on the thread count.  This input has ~9,400 strata."""
+    I, J, K = 50000, 500, 200000
+    tx, _, _, _ = bg.gen_tensor(I, J, K, 2_000_000, zipf=(1.5, 0.0, 1.5), train_frac=1.0, seed=3)
+    out = []
+    for threads in (1, 4):
+        s = bg.Schedule(bg.config(I=I, J=J, K=K, block_s=256, parallel_sequence_size=8, host_threads=threads), tx)
+        assert s.summary.num_strata > 4096
+        out.append((s.strata(), s.groups()))
+    assert out[0][0] == out[1][0]
+    for x, y in zip(out[0][1], out[1][1]):
+        assert np.array_equal(x, y)
+
+
 def test_report_byte_identical(built, tmp_path):
     c, xyz, val, s = built
     p = tmp_path / "block_parallel.txt"
