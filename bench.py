@@ -342,6 +342,8 @@ def run_gpu(args):
     traj_plain = None
     if not args.no_plain:
         for name, (dt_, md_) in (("plain", (bg.F32, bg.HOGWILD)), ("staged32", (bg.F32, bg.STAGED))):
+            if name == "staged32" and args.no_staged32:
+                continue
             c2 = bg.Context(cfg_for(w, dt_, md_, device=local), sched, tx, tv, sx, sv)
             for m in range(3):
                 c2.set_factors(m, init[m])
@@ -516,6 +518,8 @@ def main():
     ap.add_argument("--ctas", type=int, default=0, help="staged kernel CTAs per SM (0 = auto)")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner and the learned work units")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison")
+    ap.add_argument("--no-staged32", action="store_true",
+                    help="skip the untuned staged FP32 comparison (one context build less on large tensors)")
     args = ap.parse_args()
     global CTAS
     CTAS = args.ctas

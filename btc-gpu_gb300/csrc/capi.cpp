@@ -565,6 +565,41 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
         }
         if (!ts.val64.empty() && (rc = upload((void**)&c->tval64, ts.val64.data(), ts.val64.size() * 8, c->stream)))
             return rc;
+        // Per row and mode, over one epoch's executed updates: how many there
+        // are and how much regularisation decay they apply (sum of
+        // coe * lr * reg, in e-folds).  A row is FAST when that decay times a
+        // tile's share of the epoch (at most 8 CTAs per SM over the tiles)
+        // reaches 0.1: its staged updates then decay from the row's value at
+        // write time instead of the tile-start snapshot, which concurrent
+        // tiles would turn into unstable delayed feedback.  On skewed tensors
+        // only the heads of the index distributions qualify.
+        std::vector<int64_t> cnts[3];
+        std::vector<char> fast[3];
+        {
+            std::vector<double> decay[3];
+            for (int a = 0; a < 3; a++) {
+                cnts[a].assign((size_t)c->rows[a], 0);
+                decay[a].assign((size_t)c->rows[a], 0.0);
+            }
+            for (int k = 0; k < nslots; k++) {
+                double d[3];
+                for (int a = 0; a < 3; a++)
+                    d[a] = s.slot_coe[3 * (size_t)k + a] * cfg.lr * cfg.reg;
+                for (int32_t e : s.blocks[(size_t)s.slot_block[k]].ent)
+                    for (int a = 0; a < 3; a++) {
+                        const size_t r = (size_t)txyz[3 * (int64_t)e + a];
+                        cnts[a][r]++;
+                        decay[a][r] += d[a];
+                    }
+            }
+            const double share = (double)c->sms * 8.0 / (double)std::max<size_t>(1, ts.tiles.size());
+            for (int a = 0; a < 3; a++) {
+                fast[a].assign((size_t)c->rows[a], 0);
+                for (size_t r = 0; r < fast[a].size(); r++)
+                    fast[a][r] = decay[a][r] * share >= 0.1;
+            }
+        }
+        constexpr int FAST = 1 << 30;  // the kernel's flag bit in a master index
         if (c->dtype == BTC_DTYPE_BF16) {
             std::vector<int> maps[3];
             // FP32 masters for the rows whose BF16 copy would be contended:
@@ -575,10 +610,7 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
             // BF16 each time.  The other rows take at most one stochastically
             // rounded compare-and-swap per tile.
             for (int a = 0; a < 3; a++) {
-                std::vector<int64_t> cnt((size_t)c->rows[a], 0);
-                for (int k = 0; k < nslots; k++)
-                    for (int32_t e : s.blocks[(size_t)s.slot_block[k]].ent)
-                        cnt[(size_t)txyz[3 * (int64_t)e + a]]++;
+                const std::vector<int64_t>& cnt = cnts[a];
                 int64_t used = 0, total = 0;
                 for (int64_t v : cnt)
                     if (v > 0) {
@@ -600,6 +632,8 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
                 for (int64_t r = 0; r < c->rows[a]; r++)
                     if (is_hot[(size_t)r])
                         hot.push_back((int)r);
+                if (hot.size() >= (size_t)FAST)
+                    return BTC_ERR_UNSUPPORTED;
                 std::vector<int> map((size_t)c->rows[a], -1);
                 for (size_t h = 0; h < hot.size(); h++)
                     map[(size_t)hot[h]] = (int)h;
@@ -612,14 +646,24 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
                 maps[a].swap(map);
             }
             // the kernel finds a row's master in its staged row id: ~(master
-            // index) instead of the global row, so staging needs no lookup
+            // index, FAST bit for a FAST row) instead of the global row, so
+            // staging needs no lookup
             for (const btc::TileHdr& h : ts.tiles)
                 for (int r = 0; r < h.nrows; r++) {
                     const int m = r < h.nx ? 0 : (r < h.nx + h.ny ? 1 : 2);
                     int32_t& g = ts.rows[(size_t)(h.roff + r)];
                     const int hm = maps[m][(size_t)g];
                     if (hm >= 0)
-                        g = ~hm;
+                        g = ~(hm | (fast[m][(size_t)g] ? FAST : 0));
+                }
+        } else {
+            // FP32/FP64: a FAST row's staged id is ~row
+            for (const btc::TileHdr& h : ts.tiles)
+                for (int r = 0; r < h.nrows; r++) {
+                    const int m = r < h.nx ? 0 : (r < h.nx + h.ny ? 1 : 2);
+                    int32_t& g = ts.rows[(size_t)(h.roff + r)];
+                    if (fast[m][(size_t)g])
+                        g = ~g;
                 }
         }
         if ((rc = upload((void**)&c->trows, ts.rows.data(), ts.rows.size() * 4, c->stream)))

@@ -30,6 +30,11 @@ namespace btc {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
+// Staged row ids: FP32/FP64 rows hold the global row, or ~row for a FAST row
+// (decays from its value at write time); BF16 rows hold the global row when
+// they have no master, else ~(master index), with bit FAST set in the master
+// index for a FAST row.
+constexpr int FAST = 1 << 30;
 
 template <typename T>
 struct SV;
@@ -91,22 +96,25 @@ __device__ __forceinline__ float4 bf16x4_to_float4(uint2 raw)
     return make_float4(__uint_as_float(raw.x << 16), __uint_as_float(raw.x & 0xffff0000u),
                        __uint_as_float(raw.y << 16), __uint_as_float(raw.y & 0xffff0000u));
 }
-// Adds d to four consecutive BF16 elements (8 bytes, 8-byte aligned) with
-// stochastic rounding, by one 64-bit compare-and-swap per attempt.  The first
-// attempt assumes the elements still hold `guess` (the tile's snapshot of
-// them), so an uncontended row costs one round trip to L2; a stale guess only
-// costs a retry from the value the swap returned.  Element k takes random
-// bits 16k..16k+15 of (r0, r1).  Gives up (returns false) after a bounded
-// number of attempts.
-__device__ __forceinline__ bool add_quad_sr(unsigned long long* w, float4 d, unsigned r0, unsigned r1, uint2 guess)
+// Updates four consecutive BF16 elements e (8 bytes, 8-byte aligned) to
+// e + (a - c*e) with stochastic rounding, by one 64-bit compare-and-swap per
+// attempt; e is the value the swap sees, so the decay c*e uses the current
+// element.  The first attempt assumes the elements still hold `guess` (the
+// tile's snapshot of them), so an uncontended row costs one round trip to L2;
+// a stale guess only costs a retry from the value the swap returned.
+// Element k takes random bits 16k..16k+15 of (r0, r1).  Gives up (returns
+// false) after a bounded number of attempts.
+__device__ __forceinline__ float sr_step(float e, float a, float c) { return e + (a - c * e); }
+__device__ __forceinline__ bool add_quad_sr(unsigned long long* w, float4 a, float c, unsigned r0, unsigned r1,
+                                            uint2 guess)
 {
     unsigned long long old = ((unsigned long long)guess.y << 32) | guess.x;
     for (int it = 0; it < (1 << 16); it++) {
         const unsigned lo = (unsigned)old, hi = (unsigned)(old >> 32);
-        const unsigned nlo = sr_bf16_bits(__uint_as_float(lo << 16) + d.x, r0) |
-                             (sr_bf16_bits(__uint_as_float(lo & 0xffff0000u) + d.y, r0 >> 16) << 16);
-        const unsigned nhi = sr_bf16_bits(__uint_as_float(hi << 16) + d.z, r1) |
-                             (sr_bf16_bits(__uint_as_float(hi & 0xffff0000u) + d.w, r1 >> 16) << 16);
+        const unsigned nlo = sr_bf16_bits(sr_step(__uint_as_float(lo << 16), a.x, c), r0) |
+                             (sr_bf16_bits(sr_step(__uint_as_float(lo & 0xffff0000u), a.y, c), r0 >> 16) << 16);
+        const unsigned nhi = sr_bf16_bits(sr_step(__uint_as_float(hi << 16), a.z, c), r1) |
+                             (sr_bf16_bits(sr_step(__uint_as_float(hi & 0xffff0000u), a.w, c), r1 >> 16) << 16);
         const unsigned long long nw = ((unsigned long long)nhi << 32) | nlo;
         const unsigned long long prev = atomicCAS(w, old, nw);
         if (prev == old)
@@ -198,14 +206,14 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
                 unsigned short* Sb = reinterpret_cast<unsigned short*>(smem);
                 for (int i = tid; i < nc; i += blockDim.x) {
                     const int r = i / cpr, c = i - r * cpr;
-                    // the global row, or ~(master index) for a row with an FP32 master
+                    // the global row, or ~(master index | FAST) for a row with an FP32 master
                     const int g = __ldg(&a.rows[h.roff + r]);
                     const int m = r < h.nx ? 0 : (r < nxy ? 1 : 2);
                     if (c == 0)
                         rid[r] = g;
                     if (g < 0) {
                         const float* mm = m == 0 ? a.master[0] : (m == 1 ? a.master[1] : a.master[2]);
-                        const size_t hm = (size_t)(~g);
+                        const size_t hm = (size_t)(~g & (FAST - 1));
                         const float4 v0 = __ldcg(reinterpret_cast<const float4*>(mm + hm * Rp + c * 8));
                         const float4 v1 = __ldcg(reinterpret_cast<const float4*>(mm + hm * Rp + c * 8 + 4));
                         uint4 q;
@@ -223,7 +231,8 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
             }
             for (int i = tid; i < (BF ? 0 : nv); i += blockDim.x) {
                 const int r = i / vpr, c = i - r * vpr;
-                const int g = __ldg(&a.rows[h.roff + r]);
+                const int g0 = __ldg(&a.rows[h.roff + r]);  // the global row, or ~row (FAST)
+                const int g = g0 < 0 ? ~g0 : g0;
                 if constexpr (BF) {
                     // rows stay BF16 in shared memory: 16-byte chunks of 8
                     // elements, copied as they are; hot rows are rounded from
@@ -232,7 +241,7 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
                 }
                 if constexpr (!BF) {
                     if (c == 0)
-                        rid[r] = g;
+                        rid[r] = g0;
                     const T* Fm = r < h.nx ? FA : (r < nxy ? FB : FC);
                     cp16(reinterpret_cast<V*>(S) + i, reinterpret_cast<const V*>(Fm + (size_t)g * Rp) + c);
                 }
@@ -331,26 +340,35 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
                 const T* sr = S + (size_t)row * Rp;
                 const T w = m == 0 ? cx : (m == 1 ? cy : cz);
                 const T creg = (T)cnt * reg;
+                // Regularisation of a FAST row (one the host found decaying
+                // quickly relative to a tile's share of the epoch) takes the
+                // row's value at write time, not the tile-start snapshot: such
+                // a row is stepped by many concurrent tiles, and a decay
+                // computed from a value one tile old is delayed negative
+                // feedback whose gain grows with that concurrency until it
+                // diverges.  BF16 rows without a master always decay from the
+                // value their compare-and-swap sees.
                 if constexpr (BF) {
-                    const int g = rid[row];  // global row, or ~(master index)
+                    const int g = rid[row];  // global row, or ~(master index | FAST)
                     unsigned short* Fm = static_cast<unsigned short*>(m == 0 ? a.A : (m == 1 ? a.B : a.C));
 #pragma unroll
                     for (int j = 0; j < NV; j++) {
                         const int o = (j * G + gl) * VN;
                         if (MASK && o >= Rp)
                             continue;
+                        const float wc = w * creg;
+                        const float4 wa = make_float4(w * acc[j * VN + 0], w * acc[j * VN + 1],
+                                                      w * acc[j * VN + 2], w * acc[j * VN + 3]);
                         const uint2 raw = *reinterpret_cast<const uint2*>(
                             reinterpret_cast<const unsigned short*>(smem) + (size_t)row * Rp + o);
-                        const float4 own = bf16x4_to_float4(raw);
-                        float4 d;
-                        d.x = w * (acc[j * VN + 0] - creg * own.x);
-                        d.y = w * (acc[j * VN + 1] - creg * own.y);
-                        d.z = w * (acc[j * VN + 2] - creg * own.z);
-                        d.w = w * (acc[j * VN + 3] - creg * own.w);
                         if (g < 0) {
-                            float* mm = m == 0 ? a.master[0] : (m == 1 ? a.master[1] : a.master[2]);
-                            red_v(mm + (size_t)(~g) * Rp + o, d);
-                        } else if (d.x != 0.f || d.y != 0.f || d.z != 0.f || d.w != 0.f) {
+                            float* mp = (m == 0 ? a.master[0] : (m == 1 ? a.master[1] : a.master[2])) +
+                                        (size_t)(~g & (FAST - 1)) * Rp + o;
+                            const float4 base = (~g & FAST) ? __ldcg(reinterpret_cast<const float4*>(mp))
+                                                            : bf16x4_to_float4(raw);
+                            red_v(mp, make_float4(wa.x - wc * base.x, wa.y - wc * base.y, wa.z - wc * base.z,
+                                                  wa.w - wc * base.w));
+                        } else if (wa.x != 0.f || wa.y != 0.f || wa.z != 0.f || wa.w != 0.f || raw.x || raw.y) {
                             // fresh random bits for every rounding: a row without a
                             // master is written at most once per tile visit, and a
                             // block padded into several slots visits its tiles once
@@ -365,12 +383,13 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
                             const unsigned ts = mix3(seed ^ (unsigned)(m * 0x68E31DA4u), (unsigned)t, (unsigned)slot);
                             const unsigned rnd0 = mix3(ts, (unsigned)g, (unsigned)o);
                             const unsigned rnd1 = mix3(ts, (unsigned)g, (unsigned)o + 2);
-                            if (!add_quad_sr(wp, d, rnd0, rnd1, raw))
+                            if (!add_quad_sr(wp, wa, wc, rnd0, rnd1, raw))
                                 atomicExch(a.status, 1);
                         }
                     }
                 } else {
-                    T* gr = (m == 0 ? FA : (m == 1 ? FB : FC)) + (size_t)rid[row] * Rp;
+                    const int v = rid[row];  // global row, or ~row (FAST)
+                    T* gr = (m == 0 ? FA : (m == 1 ? FB : FC)) + (size_t)(v < 0 ? ~v : v) * Rp;
 #pragma unroll
                     for (int j = 0; j < NV; j++) {
                         const int o = (j * G + gl) * VN;
@@ -378,9 +397,17 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
                             continue;
                         V d;
                         T* dd = reinterpret_cast<T*>(&d);
+                        if (v < 0) {
+                            const V cur = __ldcg(reinterpret_cast<const V*>(gr + o));
+                            const T* cc = reinterpret_cast<const T*>(&cur);
 #pragma unroll
-                        for (int i = 0; i < VN; i++)
-                            dd[i] = w * (acc[j * VN + i] - creg * sr[o + i]);
+                            for (int i = 0; i < VN; i++)
+                                dd[i] = w * (acc[j * VN + i] - creg * cc[i]);
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < VN; i++)
+                                dd[i] = w * (acc[j * VN + i] - creg * sr[o + i]);
+                        }
                         red_v(gr + o, d);
                     }
                 }

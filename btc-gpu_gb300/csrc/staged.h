@@ -19,8 +19,10 @@ struct StagedArgs {
     const unsigned short* csr;
     const unsigned* segs;    // owner segments, one packed word each (row 14 bits, mode 2,
                              // count - 1 4, start in the mode's CSR list 12)
-    const int* rows;         // global row of every staged row; BF16: ~(master index)
-                             // for a row with an FP32 master
+    const int* rows;         // global row of every staged row, or ~row for a row
+                             // that decays from its value at write time; BF16:
+                             // ~(master index, bit 30 = decays at write time) for
+                             // a row with an FP32 master
     const double* val64;     // FP64 values (f64), else null
     void* A;
     void* B;
