@@ -84,6 +84,17 @@ __device__ __forceinline__ unsigned mix3(unsigned a, unsigned b, unsigned c)
     h ^= h >> 15;
     return h;
 }
+// The 32-bit finaliser of MurmurHash3 (Appleby): a bijection with full
+// avalanche, used to draw a second word of rounding bits from the first.
+__device__ __forceinline__ unsigned fmix32(unsigned h)
+{
+    h ^= h >> 16;
+    h *= 0x85EBCA6Bu;
+    h ^= h >> 13;
+    h *= 0xC2B2AE35u;
+    h ^= h >> 16;
+    return h;
+}
 __device__ __forceinline__ unsigned sr_bf16_bits(float x, unsigned r16)
 {
     unsigned u = __float_as_uint(x);
@@ -192,6 +203,8 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
             const TileHdr h = a.tiles[t];
             const int nv = h.nrows * vpr;
             const int nxy = h.nx + h.ny;
+            // rounding stream of this visit of this tile (BF16)
+            const unsigned tile_bits = BF ? mix3(seed, (unsigned)t, (unsigned)slot) : 0u;
             // the first owner segment of this lane group, fetched now so that
             // its latency hides behind staging and the errors
             const int seg_stride = nwarps * EPW;
@@ -380,9 +393,9 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
                             // The four elements are 8-byte aligned: rows start on
                             // 16 bytes (Rp is a multiple of 8) and o is a multiple of 4.
                             auto* wp = reinterpret_cast<unsigned long long*>(Fm + (size_t)g * Rp + o);
-                            const unsigned ts = mix3(seed ^ (unsigned)(m * 0x68E31DA4u), (unsigned)t, (unsigned)slot);
-                            const unsigned rnd0 = mix3(ts, (unsigned)g, (unsigned)o);
-                            const unsigned rnd1 = mix3(ts, (unsigned)g, (unsigned)o + 2);
+                            const unsigned rnd0 =
+                                mix3(tile_bits ^ (unsigned)(m * 0x68E31DA4u), (unsigned)g, (unsigned)o);
+                            const unsigned rnd1 = fmix32(rnd0 ^ 0x5BD1E995u);
                             if (!add_quad_sr(wp, wa, wc, rnd0, rnd1, raw))
                                 atomicExch(a.status, 1);
                         }
@@ -412,8 +425,10 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
                     }
                 }
             }
-            // the slot's next tile must see these adds
-            __threadfence();
+            // the slot's next tile must see these adds (nothing orders the
+            // adds of different slots, so the last tile needs no fence)
+            if (t + 1 < t1)
+                __threadfence();
             __syncthreads();
             if (a.tile_ns && tid == 0) {
                 unsigned long long t_end;
