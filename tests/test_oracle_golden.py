@@ -80,6 +80,31 @@ def test_fixtures_cover_quirks():
     assert all(seen.values()), seen
 
 
+def test_flat_schedule_sample_is_a_prefix(case):
+    """The CPU legs of the bench replay a bounded leading sample of large
+    schedules: that sample is the full schedule's first groups, and replaying
+    it gives exactly the factors of replaying those groups of the full one."""
+    c, s = case
+    full = oracle.FlatSchedule(s.group_off, s.slot_ids, s.slot_coe, lambda b: s.block_entries[b])
+    if full.nslots < 2:
+        pytest.skip("single-slot schedule")
+    cap = int(full.soff[full.nslots // 2])
+    part = oracle.FlatSchedule(s.group_off, s.slot_ids, s.slot_coe, lambda b: s.block_entries[b],
+                               max_updates=cap)
+    assert 0 < part.ngroups <= full.ngroups and part.soff[-1] >= cap
+    assert np.array_equal(part.goff, full.goff[: part.ngroups + 1])
+    assert np.array_equal(part.soff, full.soff[: part.nslots + 1])
+    assert np.array_equal(part.ent, full.ent[: len(part.ent)])
+    R = 4
+    rng = np.random.default_rng(1)
+    F1 = [rng.uniform(0, 0.1, (n, R)) for n in c.dims]
+    F2 = [f.copy() for f in F1]
+    val = c.shuffled_values()
+    u1 = full.replay(c.shuffled, val, R, 0.01, 0.01, *F1, 0, part.nslots)
+    u2 = part.replay(c.shuffled, val, R, 0.01, 0.01, *F2)
+    assert u1 == u2 and all(np.array_equal(a, b) for a, b in zip(F1, F2))
+
+
 def test_hx_float_rounding():
     """hx divides in float: near the top of a 5M axis the bucket differs from
     the exact integer quotient (block.cu:41-42)."""
