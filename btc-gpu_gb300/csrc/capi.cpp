@@ -605,10 +605,10 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
             // FP32 masters for the rows whose BF16 copy would be contended:
             // every row that a tile updates through more than one owner
             // segment (those segments add to it concurrently) and every row
-            // updated at least 4x as often as the mean row; their small
-            // updates then accumulate exactly instead of being rounded to
-            // BF16 each time.  The other rows take at most one stochastically
-            // rounded compare-and-swap per tile.
+            // updated at least 4x as often as the mean row, and every FAST
+            // row; their small updates then accumulate exactly instead of
+            // being rounded to BF16 each time.  The other rows take at most
+            // one stochastically rounded update per tile visit.
             for (int a = 0; a < 3; a++) {
                 const std::vector<int64_t>& cnt = cnts[a];
                 int64_t used = 0, total = 0;
@@ -630,7 +630,7 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
                     }
                 std::vector<int> hot;
                 for (int64_t r = 0; r < c->rows[a]; r++)
-                    if (is_hot[(size_t)r])
+                    if (is_hot[(size_t)r] || fast[a][(size_t)r])  // FAST rows decay from their master
                         hot.push_back((int)r);
                 if (hot.size() >= (size_t)FAST)
                     return BTC_ERR_UNSUPPORTED;

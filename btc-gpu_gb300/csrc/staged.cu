@@ -11,9 +11,9 @@
 //              sharing a row of one mode) sums err * (other two rows) from S
 //              in registers and adds coe*lr*(sum - count*reg*row) to the row
 //              in global memory with one vector atomic per 16 bytes (BF16
-//              rows without a master: one stochastically rounding 8-byte
-//              compare-and-swap per 4 elements), so a row is written once per
-//              segment instead of once per entry.
+//              rows without a master: the stochastically rounded difference
+//              to the snapshot, by bf16x2 atomic adds), so a row is written
+//              once per segment instead of once per entry.
 // Inside a tile the update is the reference kernel's: all entries of one
 // thread_size wave read rows before their deltas land (sgd_Kernel.cu:358-392),
 // coe-weighted, L2-regularised per visit.  Tiles of one slot run in order on
@@ -107,33 +107,8 @@ __device__ __forceinline__ float4 bf16x4_to_float4(uint2 raw)
     return make_float4(__uint_as_float(raw.x << 16), __uint_as_float(raw.x & 0xffff0000u),
                        __uint_as_float(raw.y << 16), __uint_as_float(raw.y & 0xffff0000u));
 }
-// Updates four consecutive BF16 elements e (8 bytes, 8-byte aligned) to
-// e + (a - c*e) with stochastic rounding, by one 64-bit compare-and-swap per
-// attempt; e is the value the swap sees, so the decay c*e uses the current
-// element.  The first attempt assumes the elements still hold `guess` (the
-// tile's snapshot of them), so an uncontended row costs one round trip to L2;
-// a stale guess only costs a retry from the value the swap returned.
-// Element k takes random bits 16k..16k+15 of (r0, r1).  Gives up (returns
-// false) after a bounded number of attempts.
+// One element's update e + (a - c*e): the step with its decay term.
 __device__ __forceinline__ float sr_step(float e, float a, float c) { return e + (a - c * e); }
-__device__ __forceinline__ bool add_quad_sr(unsigned long long* w, float4 a, float c, unsigned r0, unsigned r1,
-                                            uint2 guess)
-{
-    unsigned long long old = ((unsigned long long)guess.y << 32) | guess.x;
-    for (int it = 0; it < (1 << 16); it++) {
-        const unsigned lo = (unsigned)old, hi = (unsigned)(old >> 32);
-        const unsigned nlo = sr_bf16_bits(sr_step(__uint_as_float(lo << 16), a.x, c), r0) |
-                             (sr_bf16_bits(sr_step(__uint_as_float(lo & 0xffff0000u), a.y, c), r0 >> 16) << 16);
-        const unsigned nhi = sr_bf16_bits(sr_step(__uint_as_float(hi << 16), a.z, c), r1) |
-                             (sr_bf16_bits(sr_step(__uint_as_float(hi & 0xffff0000u), a.w, c), r1 >> 16) << 16);
-        const unsigned long long nw = ((unsigned long long)nhi << 32) | nlo;
-        const unsigned long long prev = atomicCAS(w, old, nw);
-        if (prev == old)
-            return true;
-        old = prev;
-    }
-    return false;
-}
 
 __device__ __forceinline__ float4 ld_bf4(const unsigned short* p)
 {
@@ -307,7 +282,7 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
             }
             __syncthreads();
             // 3. owner segments: reduce in registers, one vector add per 16 bytes
-            //    (BF16: one 8-byte compare-and-swap per 4 elements)
+            //    (BF16 without a master: two bf16x2 adds per 4 elements)
             for (int s0 = warp * EPW; s0 < h.nseg; s0 += seg_stride) {
                 const int s = s0 + sub;
                 const unsigned sg = sg_next;
@@ -359,8 +334,7 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
                 // a row is stepped by many concurrent tiles, and a decay
                 // computed from a value one tile old is delayed negative
                 // feedback whose gain grows with that concurrency until it
-                // diverges.  BF16 rows without a master always decay from the
-                // value their compare-and-swap sees.
+                // diverges.  In BF16 every FAST row has a master.
                 if constexpr (BF) {
                     const int g = rid[row];  // global row, or ~(master index | FAST)
                     unsigned short* Fm = static_cast<unsigned short*>(m == 0 ? a.A : (m == 1 ? a.B : a.C));
@@ -390,14 +364,25 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
                             // updates of an epoch would round an element the same
                             // way every time and let its magnitude drift by up to
                             // one ulp per update.
-                            // The four elements are 8-byte aligned: rows start on
-                            // 16 bytes (Rp is a multiple of 8) and o is a multiple of 4.
-                            auto* wp = reinterpret_cast<unsigned long long*>(Fm + (size_t)g * Rp + o);
+                            // The new value is computed from the snapshot and rounded
+                            // stochastically; its difference to the snapshot (a few
+                            // ulps, exact in BF16) lands by fire-and-forget bf16x2
+                            // atomic adds, skipped when the rounding left the pair
+                            // unchanged.  With no other tile on the row since the
+                            // snapshot the result is exactly the rounded value.
+                            __nv_bfloat162* wp = reinterpret_cast<__nv_bfloat162*>(Fm + (size_t)g * Rp + o);
                             const unsigned rnd0 =
                                 mix3(tile_bits ^ (unsigned)(m * 0x68E31DA4u), (unsigned)g, (unsigned)o);
                             const unsigned rnd1 = fmix32(rnd0 ^ 0x5BD1E995u);
-                            if (!add_quad_sr(wp, wa, wc, rnd0, rnd1, raw))
-                                atomicExch(a.status, 1);
+                            const float4 own = bf16x4_to_float4(raw);
+                            const float n0 = __uint_as_float(sr_bf16_bits(sr_step(own.x, wa.x, wc), rnd0) << 16);
+                            const float n1 = __uint_as_float(sr_bf16_bits(sr_step(own.y, wa.y, wc), rnd0 >> 16) << 16);
+                            const float n2 = __uint_as_float(sr_bf16_bits(sr_step(own.z, wa.z, wc), rnd1) << 16);
+                            const float n3 = __uint_as_float(sr_bf16_bits(sr_step(own.w, wa.w, wc), rnd1 >> 16) << 16);
+                            if (n0 != own.x || n1 != own.y)
+                                atomicAdd(wp, __floats2bfloat162_rn(n0 - own.x, n1 - own.y));
+                            if (n2 != own.z || n3 != own.w)
+                                atomicAdd(wp + 1, __floats2bfloat162_rn(n2 - own.z, n3 - own.w));
                         }
                     }
                 } else {

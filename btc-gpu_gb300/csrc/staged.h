@@ -35,7 +35,8 @@ struct StagedArgs {
     // BF16 storage only
     float* master[3];        // FP32 master rows of the hottest rows of each mode
     unsigned seed;           // stochastic-rounding stream of this epoch
-    int* status;             // set to 1 when a rounding compare-and-swap gives up
+    int* status;             // device error word read after each epoch (no current
+                             // kernel path sets it)
     unsigned* tile_ns;       // when set: nanoseconds each tile took (globaltimer)
     int G, NV;               // lane-group shape; 0 = the default for the rank
     const unsigned* seed_ptr;  // when set, the rounding stream is seed ^ *seed_ptr (graph replays)
