@@ -67,7 +67,7 @@ SEED = 20261203 + 1
 CTAS = 0
 # DRAM bytes per launch of the timed kernel from an ncu capture of the same
 # workload (profiles/), keyed by (workload, dtype, mode); absent = null
-TRAFFIC = {("c2", "f32", "staged"): 1.556e9, ("c2", "f32", "hogwild"): 0.7786e9, ("c2", "bf16", "staged"): 1.368e9}
+TRAFFIC = {("c2", "f32", "staged"): 1.556e9, ("c2", "f32", "hogwild"): 0.7786e9, ("c2", "bf16", "staged"): 1.366e9}
 
 
 def log(*a):
