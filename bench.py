@@ -294,7 +294,7 @@ def run_gpu(args):
     if mode == bg.STAGED and not args.no_tune:
         tune = ctx.autotune(2)
         model = bg.MLP()
-        learn = ctx.learn_work_units(model, train_steps=300, judge_epochs=2)
+        learn = ctx.learn_work_units(model, train_steps=300, trial_epochs=2)
         model.close()
         log("autotune: G=%d NV=%d ctas/SM=%d (%d candidates) %.3f -> %.3f ms; learned units: %d, R2 %.3f, "
             "plain %.3f ms learned %.3f ms kept %d" % (tune.lanes_per_entry, tune.vectors_per_lane,

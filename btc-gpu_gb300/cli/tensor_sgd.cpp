@@ -10,7 +10,7 @@
 //              [--parallel-sequence-size|--parallel_sequence_size N]
 //              [--gpus|--gpu-count|--gpu_count N]
 //
-// Options this build adds (none collide with the reference's):
+// Options added to the reference's command line (none collide with its own):
 //   --precision f32|f64|bf16   factor storage / math (default f32)
 //   --mode hogwild|deterministic|staged   kernel schedule (default hogwild)
 //   --seed N                   seeded U(init-lo, init-hi) factor init; without it
@@ -462,7 +462,7 @@ int main(int argc, char** argv)
         cout << "requested_gpus=" << cfg.requested_gpu_count << " exceeds visible GPU count; using " << active
              << " GPU(s)." << endl;
     if (active > 1)
-        cout << "This build trains on one GPU; using GPU[" << cfg.device << "]." << endl;
+        cout << "Training on one GPU; using GPU[" << cfg.device << "]." << endl;
     cout << "Using 1 GPU(s) for training." << endl;
     std::ofstream ofs_error((dir + "error.txt").c_str(), std::ios::out | std::ios::trunc);
     std::ofstream ofs_time((dir + "time.txt").c_str(), std::ios::out | std::ios::trunc);

@@ -1000,12 +1000,12 @@ btc_status btc_ctx_slot_tiles(btc_ctx* c, int32_t* tile0, int32_t* ntiles)
 //             set-up); consecutive slots are packed into units of about equal
 //             predicted cost, at least 8 per CTA so that no CTA is left with a
 //             long last unit;
-// 4. judge    epochs with the proposed units and with one slot per unit are
+// 4. trial    epochs with the proposed units and with one slot per unit are
 //             timed alternately; the faster packing stays.
-btc_status btc_ctx_learn_work_units(btc_ctx* c, btc_mlp* model, int32_t train_steps, int32_t judge_epochs,
+btc_status btc_ctx_learn_work_units(btc_ctx* c, btc_mlp* model, int32_t train_steps, int32_t trial_epochs,
                                     btc_learn_report* rep)
 {
-    if (!c || !model || train_steps < 0 || judge_epochs < 1 || !rep || c->mode != BTC_MODE_STAGED)
+    if (!c || !model || train_steps < 0 || trial_epochs < 1 || !rep || c->mode != BTC_MODE_STAGED)
         return BTC_ERR_ARG;
     btc_learn_report r{};
     const int64_t ntiles = c->st_tiles;
@@ -1073,9 +1073,9 @@ btc_status btc_ctx_learn_work_units(btc_ctx* c, btc_mlp* model, int32_t train_st
         }
     }
     r.units = (int32_t)units.size() - 1;
-    // judge: alternate the two packings
+    // trial: alternate the two packings
     double t_plain = 0, t_learn = 0;
-    for (int e = 0; e < judge_epochs; e++) {
+    for (int e = 0; e < trial_epochs; e++) {
         btc_epoch_stats a{}, b{};
         if ((rc = btc_ctx_set_work_units(c, plain.data(), c->nslots)) || (rc = btc_train_epoch(c, &a)))
             return rc;
@@ -1084,8 +1084,8 @@ btc_status btc_ctx_learn_work_units(btc_ctx* c, btc_mlp* model, int32_t train_st
         t_plain += a.kernel_ms;
         t_learn += b.kernel_ms;
     }
-    r.plain_ms = t_plain / judge_epochs;
-    r.learned_ms = t_learn / judge_epochs;
+    r.plain_ms = t_plain / trial_epochs;
+    r.learned_ms = t_learn / trial_epochs;
     r.kept = r.learned_ms < r.plain_ms ? 1 : 0;
     if (!r.kept && (rc = btc_ctx_set_work_units(c, plain.data(), c->nslots)))
         return rc;

@@ -468,9 +468,9 @@ class Context:
         u = np.ascontiguousarray(unit_off, np.int32)
         _ck(_lib().btc_ctx_set_work_units(self._h, _p(u), len(u) - 1), "btc_ctx_set_work_units")
 
-    def learn_work_units(self, model, train_steps=300, judge_epochs=3):
+    def learn_work_units(self, model, train_steps=300, trial_epochs=3):
         r = LearnReport()
-        _ck(_lib().btc_ctx_learn_work_units(self._h, model.handle, train_steps, judge_epochs, ctypes.byref(r)),
+        _ck(_lib().btc_ctx_learn_work_units(self._h, model.handle, train_steps, trial_epochs, ctypes.byref(r)),
             "btc_ctx_learn_work_units")
         return r
 

@@ -38,7 +38,7 @@ typedef enum btc_status {
     BTC_ERR_STATE = 4,       /* call out of order / object in a failed state */
     BTC_ERR_IO = 5,          /* file could not be opened, read or written */
     BTC_ERR_TIMEOUT = 6,     /* a bounded device wait gave up */
-    BTC_ERR_UNSUPPORTED = 7, /* valid request this build does not implement */
+    BTC_ERR_UNSUPPORTED = 7, /* valid request this library does not implement */
     BTC_ERR_RANGE = 8,       /* index or level outside the representable range */
     BTC_ERR_NO_DEVICE = 9,   /* no CUDA device visible */
     BTC_ERR_DEVICE = 10      /* a kernel reported an error status */
@@ -68,7 +68,7 @@ typedef enum btc_mode {
 typedef enum btc_split { BTC_SPLIT_TRAIN = 0, BTC_SPLIT_TEST = 1 } btc_split;
 
 /* Configuration: the reference's globals (tensor_SGD.h:25-42, defaults in
- * tensor_SGD.cu:24-41) plus the options this build adds. */
+ * tensor_SGD.cu:24-41) plus the options this library adds. */
 typedef struct btc_config {
     int32_t I, J, K;                /* mode sizes */
     int32_t epochs;                 /* default 1000 */
@@ -78,7 +78,7 @@ typedef struct btc_config {
     int32_t block_s;                /* block capacity, default 2048 */
     int32_t thread_size;            /* accepted for compatibility, default 512 */
     int32_t parallel_sequence_size; /* blocks per stratum on the GPU; 0 = auto; default 8 */
-    int32_t requested_gpu_count;    /* accepted; this build always uses one GPU */
+    int32_t requested_gpu_count;    /* accepted; the library always uses one GPU */
     int32_t dtype;                  /* btc_dtype, default BTC_DTYPE_F32 */
     int32_t mode;                   /* btc_mode, default BTC_MODE_HOGWILD */
     int32_t device;                 /* CUDA device ordinal, default 0 */
@@ -236,9 +236,9 @@ typedef struct btc_learn_report {
     int32_t units;        /* work units proposed */
     int32_t kept;         /* 1: the proposed units were kept; 0: the heuristic stayed */
 } btc_learn_report;
-/* profile one epoch, train `model`, propose units, time judge_epochs epochs of
+/* profile one epoch, train `model`, propose units, time trial_epochs epochs of
  * each (they are training epochs) and keep the faster */
-btc_status btc_ctx_learn_work_units(btc_ctx *ctx, btc_mlp *model, int32_t train_steps, int32_t judge_epochs,
+btc_status btc_ctx_learn_work_units(btc_ctx *ctx, btc_mlp *model, int32_t train_steps, int32_t trial_epochs,
                                     btc_learn_report *report);
 
 /* ---- autotuner -------------------------------------------------------------

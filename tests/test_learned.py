@@ -32,7 +32,7 @@ def test_mlp_learns_a_smooth_cost():
     assert np.abs(pred - y).mean() < 0.15
 
 
-def test_learned_work_units_are_judged_by_epoch_time():
+def test_learned_work_units_are_kept_only_if_faster():
     tx, tv, sx, sv = bg.gen_tensor(20000, 20000, 5000, 600000, zipf=(1.2, 1.2, 1.2), gt_rank=8, seed=5)
     tx, tv = bg.shuffle(tx, tv)
     cfg = bg.config(I=20000, J=20000, K=5000, rank=32, lr=0.005, reg=0.02, block_s=2048, mode=bg.STAGED)
@@ -41,7 +41,7 @@ def test_learned_work_units_are_judged_by_epoch_time():
     ctx.init_factors(1, 0.0, 0.1)
     ctx.train_epochs(2)
     model = bg.MLP()
-    r = ctx.learn_work_units(model, train_steps=300, judge_epochs=3)
+    r = ctx.learn_work_units(model, train_steps=300, trial_epochs=3)
     assert r.samples > 100 and r.units > 0
     assert r.model_r2 > 0.3
     assert r.kept == (1 if r.learned_ms < r.plain_ms else 0)
