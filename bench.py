@@ -199,7 +199,7 @@ def run_reference(args):
     sched = bg.Schedule(cfg, tx)
     flat = flat_schedule(sched)
     threads = os.cpu_count() or 1
-    per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup))
+    per_step = max(min(2.0, args.ref_seconds), args.ref_seconds / max(1, args.steps + args.warmup))
     for _ in range(args.warmup):
         cpu_sample(flat, tx, tv, w, per_step / 4, threads)
     ups, times = [], []
@@ -221,19 +221,23 @@ def run_reference(args):
     return 0
 
 
+def _max_over_ranks(x, dist):
+    """The largest of every rank's x (x itself without a process group)."""
+    if not dist:
+        return x
+    import torch
+
+    tt = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
 def _timed(ctx, steps, dist):
     """K back-to-back epochs between barriers; device ms (max over ranks)."""
     if dist:
         dist.barrier()
     st = ctx.train_epochs(steps)
-    ms = st.kernel_ms
-    if dist:
-        import torch
-
-        tt = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    return st, ms
+    return st, _max_over_ranks(st.kernel_ms, dist)
 
 
 def _trajectory(ctx, w, epochs):
@@ -321,13 +325,7 @@ def run_gpu(args):
     t = time.perf_counter()
     for _ in range(e2e_steps):
         _, met = ctx.train_epoch_host(*(p_.array for p_ in pinned))
-    e2e_s = time.perf_counter() - t
-    if dist:
-        import torch
-
-        tt = torch.tensor([e2e_s], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = _max_over_ranks(time.perf_counter() - t, dist)
     fac_bytes = sum(n * w["R"] * 8 for n in (w["I"], w["J"], w["K"]))
     e2e = {"value": upd_per_step * e2e_steps * world / e2e_s, "unit": "updates/s",
            "h2d_bytes_per_step": fac_bytes, "d2h_bytes_per_step": fac_bytes + 24}
@@ -515,6 +513,8 @@ def main():
     ap.add_argument("--dtype", default="bf16", choices=["f32", "f64", "bf16"])
     ap.add_argument("--mode", default="staged", choices=["hogwild", "deterministic", "staged"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-seconds", type=float, default=60.0,
+                    help="host-core time the reference arm spreads over its warm-up and timed steps")
     ap.add_argument("--ctas", type=int, default=0, help="staged kernel CTAs per SM (0 = auto)")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner and the learned work units")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison")
