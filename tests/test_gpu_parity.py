@@ -114,6 +114,30 @@ def test_empty_test_split_gives_nan():
     assert m.count == 0 and np.isnan(m.rmse) and np.isnan(m.mae) and np.isnan(m.er)
 
 
+@pytest.mark.parametrize("dtype,mode", [(bg.F32, bg.HOGWILD), (bg.F64, bg.DETERMINISTIC), (bg.F32, bg.STAGED),
+                                        (bg.BF16, bg.STAGED)])
+def test_empty_train_split_epochs_are_no_ops(dtype, mode):
+    """No training entries: the schedule is empty, an epoch executes no update
+    and leaves the factors as they were, and the test split still evaluates."""
+    c, xyz, val, init, sched = _setup("uniform_3k", 8)
+    I, J, K = c.dims
+    cfg = bg.config(I=I, J=J, K=K, rank=8, lr=LR, reg=REG, block_s=c.meta["block_s"], dtype=dtype, mode=mode)
+    empty = np.zeros((0, 3), np.int32)
+    s = bg.Schedule(cfg, empty)
+    assert s.summary.num_slots == 0 and s.summary.scheduled_updates == 0
+    ctx = bg.Context(cfg, s, empty, np.zeros(0), xyz, val)
+    for m in range(3):
+        ctx.set_factors(m, init[m])
+    before = [ctx.get_factors(m) for m in range(3)]
+    st = ctx.train_epochs(2)
+    assert st.updates == 0 and st.device_status == 0
+    for m in range(3):
+        assert np.array_equal(ctx.get_factors(m), before[m])
+    mt = ctx.eval(bg.TEST)
+    assert mt.count == len(val) and np.isfinite(mt.rmse)
+    ctx.close()
+
+
 def test_factor_roundtrip_and_init():
     c, xyz, val, init, sched = _setup("uniform_3k", 24)
     for dtype in (bg.F32, bg.F64):
