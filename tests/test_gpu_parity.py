@@ -114,6 +114,26 @@ def test_empty_test_split_gives_nan():
     assert m.count == 0 and np.isnan(m.rmse) and np.isnan(m.mae) and np.isnan(m.er)
 
 
+@pytest.mark.parametrize("R", [1, 128])
+@pytest.mark.parametrize("dtype,mode,tol", [(bg.F32, bg.HOGWILD, 2e-3), (bg.F32, bg.STAGED, 2e-3),
+                                            (bg.BF16, bg.STAGED, 2e-2)])
+def test_rank_extremes_close_to_serial(R, dtype, mode, tol):
+    """The smallest and the largest rank the library accepts (1 and 128)
+    take the same kernels' padded and widest lane shapes."""
+    c, xyz, val, init, sched = _setup("zipf13_6k", R)
+    ref = [m.copy() for m in init]
+    ctx = _ctx(c, xyz, val, R, dtype, mode)
+    for m in range(3):
+        ctx.set_factors(m, init[m])
+    for epoch in range(3):
+        sched.sgd_epoch(val, R, LR, REG, *ref)
+        st = ctx.train_epoch()
+        assert st.device_status == 0
+        rmse = ctx.eval(bg.TEST).rmse
+        want = oracle.rmse_mae_er(xyz, val, R, *ref)[0]
+        assert abs(rmse - want) / want <= tol, (epoch, rmse, want)
+
+
 @pytest.mark.parametrize("dtype,mode", [(bg.F32, bg.HOGWILD), (bg.F64, bg.DETERMINISTIC), (bg.F32, bg.STAGED),
                                         (bg.BF16, bg.STAGED)])
 def test_empty_train_split_epochs_are_no_ops(dtype, mode):
