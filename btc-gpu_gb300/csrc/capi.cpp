@@ -1284,6 +1284,8 @@ struct btc_batch {
     int2* items = nullptr;
     int* counter = nullptr;
     unsigned* seed = nullptr;
+    btc::RefreshJob* refresh = nullptr;  // BF16: one master refresh job per (context, mode) with hot rows
+    int nrefresh = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int64_t updates = 0;
@@ -1305,6 +1307,7 @@ btc_status btc_batch_destroy(btc_batch* b)
     free_dev(b->items);
     free_dev(b->counter);
     free_dev(b->seed);
+    free_dev(b->refresh);
     if (b->ev0)
         cudaEventDestroy(b->ev0);
     if (b->ev1)
@@ -1360,6 +1363,17 @@ static btc_status batch_build(btc_batch* b)
     if ((rc = upload((void**)&b->items, items.data(), items.size() * sizeof(int2), b->stream)))
         return rc;
     CK(cudaMalloc((void**)&b->counter, sizeof(int)));
+    if (b->dtype == BTC_DTYPE_BF16) {
+        std::vector<btc::RefreshJob> jobs;
+        for (btc_ctx* c : b->ctx)
+            for (int a = 0; a < 3; a++)
+                if (c->nhot[a] > 0)
+                    jobs.push_back({c->master[a], static_cast<unsigned short*>(c->F[a]), c->hot_rows[a], c->nhot[a],
+                                    c->Rp});
+        b->nrefresh = (int)jobs.size();
+        if ((rc = upload((void**)&b->refresh, jobs.data(), jobs.size() * sizeof(btc::RefreshJob), b->stream)))
+            return rc;
+    }
     int occ = btc::staged_multi_blocks_per_sm(b->dtype, b->smem);
     if (occ <= 0)
         return BTC_ERR_UNSUPPORTED;
@@ -1409,14 +1423,10 @@ static btc_status batch_enqueue(btc_batch* b, int* launches)
     CK(cudaMemsetAsync(b->counter, 0, sizeof(int), b->stream));
     CK(btc::launch_staged_multi(b->dtype, b->args, b->items, b->nitems, b->counter, b->smem, b->grid, b->stream));
     n++;
-    if (b->dtype == BTC_DTYPE_BF16) {
-        for (btc_ctx* c : b->ctx)
-            for (int a = 0; a < 3; a++)
-                if (c->nhot[a] > 0) {
-                    CK(btc::launch_master(2, nullptr, nullptr, c->master[a], c->F[a], c->hot_rows[a], c->nhot[a],
-                                          c->R, c->Rp, b->stream));
-                    n++;
-                }
+    if (b->nrefresh > 0) {
+        // every context's BF16 copies of its hot rows, in one launch
+        CK(btc::launch_master_refresh_multi(b->refresh, b->nrefresh, b->stream));
+        n++;
     }
     CK(btc::launch_seed_step(b->seed, b->stream));
     n++;

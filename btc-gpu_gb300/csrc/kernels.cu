@@ -473,6 +473,18 @@ __global__ void k_master_refresh(const float* master, unsigned short* dst, const
     }
 }
 
+// k_master_refresh for many contexts: blockIdx.y picks the job.
+__global__ void k_master_refresh_multi(const RefreshJob* jobs)
+{
+    const RefreshJob j = jobs[blockIdx.y];
+    const long long n = (long long)j.nhot * j.Rp;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int h = (int)(i / j.Rp), c = (int)(i - (long long)h * j.Rp);
+        j.bf16[(long long)j.hot_rows[h] * j.Rp + c] = __bfloat16_as_ushort(__float2bfloat16_rn(j.master[i]));
+    }
+}
+
 __global__ void k_seed_step(unsigned* p) { *p += 0x9E3779B9u; }
 
 int grid_for(long long n)
@@ -481,6 +493,16 @@ int grid_for(long long n)
 }
 
 }  // namespace
+
+cudaError_t launch_master_refresh_multi(const RefreshJob* jobs, int njobs, cudaStream_t st)
+{
+    if (njobs <= 0)
+        return cudaSuccess;
+    if (njobs > 65535)
+        return cudaErrorInvalidValue;
+    k_master_refresh_multi<<<dim3(64, njobs), 256, 0, st>>>(jobs);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_seed_step(unsigned* p, cudaStream_t st)
 {

@@ -48,6 +48,15 @@ constexpr int kMetricThreads = 256;
 // refreshes the BF16 copy of every hot row from its master.
 cudaError_t launch_master(int op, const double* src, double* dst, float* master, void* bf16, const int* hot_rows,
                           int nhot, int R, int Rp, cudaStream_t st);
+// The op-2 refresh of many BF16 contexts in one launch: one job per (context,
+// mode) with hot rows.
+struct RefreshJob {
+    const float* master;
+    unsigned short* bf16;
+    const int* hot_rows;
+    int nhot, Rp;
+};
+cudaError_t launch_master_refresh_multi(const RefreshJob* jobs, int njobs, cudaStream_t st);
 // Advances a device-side rounding seed (one step per replayed epoch).
 cudaError_t launch_seed_step(unsigned* p, cudaStream_t st);
 // double [rows][R] <-> padded device rows [rows][Rp] of the dtype
