@@ -11,21 +11,22 @@
 
 #include <algorithm>
 #include <cstring>
+#include <thread>
 
 namespace btc {
+namespace {
 
-void build_tiles(const Schedule& s, const int32_t* xyz, const double* val, int I, int J, int K, int cap,
-                 int wave, int seg, bool want64, TileSet& out)
+// The tiles of blocks blk[0..nb), in that order, into `out` (offsets local
+// to `out`); first[i] / count[i] receive block blk[i]'s first tile and tile
+// count.
+void build_range(const Schedule& s, const int32_t* xyz, const double* val, const int* dims, int cap, int wave,
+                 int seg, bool want64, const int* blk, size_t nb, TileSet& out, int* first, int* count)
 {
-    out = TileSet();
-    const int dims[3] = {I, J, K};
     std::vector<int> stamp[3], loc[3];
     for (int a = 0; a < 3; a++) {
         stamp[a].assign((size_t)dims[a], -1);
         loc[a].assign((size_t)dims[a], 0);
     }
-    out.block_tile0.assign(s.blocks.size(), -1);
-    out.block_ntiles.assign(s.blocks.size(), 0);
     int tile_id = 0;
     std::vector<int32_t> rows_m[3];
     struct Ent {
@@ -97,11 +98,9 @@ void build_tiles(const Schedule& s, const int32_t* xyz, const double* val, int I
         tile_id++;
     };
 
-    for (size_t k = 0; k < s.slot_block.size(); k++) {
-        const int b = s.slot_block[k];
-        if (out.block_tile0[(size_t)b] >= 0)
-            continue;
-        out.block_tile0[(size_t)b] = (int)out.tiles.size();
+    for (size_t i = 0; i < nb; i++) {
+        const int b = blk[i];
+        first[i] = (int)out.tiles.size();
         for (int32_t e : s.blocks[(size_t)b].ent) {
             const int32_t* c = xyz + 3 * (int64_t)e;
             int need = 0;
@@ -124,8 +123,122 @@ void build_tiles(const Schedule& s, const int32_t* xyz, const double* val, int I
             cur.push_back(q);
         }
         close();
-        out.block_ntiles[(size_t)b] = (int)out.tiles.size() - out.block_tile0[(size_t)b];
+        count[i] = (int)out.tiles.size() - first[i];
     }
+}
+
+}  // namespace
+
+// Blocks are tiled independently (a tile never spans two blocks), so the
+// blocks, in order of first use by the slots, are split into contiguous
+// runs of about equal entry count, one per thread, and the runs' tile sets
+// are concatenated in order with their offsets moved: the result does not
+// depend on the thread count.
+void build_tiles(const Schedule& s, const int32_t* xyz, const double* val, int I, int J, int K, int cap,
+                 int wave, int seg, bool want64, TileSet& out, int threads)
+{
+    out = TileSet();
+    const int dims[3] = {I, J, K};
+    out.block_tile0.assign(s.blocks.size(), -1);
+    out.block_ntiles.assign(s.blocks.size(), 0);
+    std::vector<int> order;
+    std::vector<long long> ent_before(1, 0);
+    {
+        std::vector<char> seen(s.blocks.size(), 0);
+        for (int b : s.slot_block)
+            if (!seen[(size_t)b]) {
+                seen[(size_t)b] = 1;
+                order.push_back(b);
+                ent_before.push_back(ent_before.back() + (long long)s.blocks[(size_t)b].ent.size());
+            }
+    }
+    const long long total = ent_before.back();
+    int T = std::max(1, std::min(threads, 64));
+    if (total < (1LL << 20))
+        T = 1;  // small inputs: one run
+    std::vector<size_t> cut((size_t)T + 1, 0);
+    for (int t = 1; t < T; t++)
+        cut[(size_t)t] = (size_t)(std::lower_bound(ent_before.begin(), ent_before.end(), total * t / T) -
+                                  ent_before.begin());
+    cut[(size_t)T] = order.size();
+    for (int t = 1; t <= T; t++)
+        cut[(size_t)t] = std::max(cut[(size_t)t], cut[(size_t)t - 1]);
+    std::vector<TileSet> part((size_t)T);
+    std::vector<int> first(order.size()), count(order.size());
+    auto work = [&](int t) {
+        const size_t lo = cut[(size_t)t], hi = cut[(size_t)t + 1];
+        build_range(s, xyz, val, dims, cap, wave, seg, want64, order.data() + lo, hi - lo, part[(size_t)t],
+                    first.data() + lo, count.data() + lo);
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < T; t++)
+        pool.emplace_back(work, t);
+    work(0);
+    for (auto& th : pool)
+        th.join();
+    for (int t = 0; t < T; t++) {
+        int tile_base = 0;
+        for (int u = 0; u < t; u++)
+            tile_base += (int)part[(size_t)u].tiles.size();
+        for (size_t i = cut[(size_t)t]; i < cut[(size_t)t + 1]; i++) {
+            out.block_tile0[(size_t)order[i]] = tile_base + first[i];
+            out.block_ntiles[(size_t)order[i]] = count[i];
+        }
+        out.max_rows = std::max(out.max_rows, part[(size_t)t].max_rows);
+        out.max_n = std::max(out.max_n, part[(size_t)t].max_n);
+    }
+    if (T == 1) {  // one run: its offsets are already the final ones
+        out.tiles.swap(part[0].tiles);
+        out.ent.swap(part[0].ent);
+        out.csr.swap(part[0].csr);
+        out.segs.swap(part[0].segs);
+        out.rows.swap(part[0].rows);
+        out.val64.swap(part[0].val64);
+        return;
+    }
+    // runs are copied into place in parallel, each run's offsets moved by the
+    // sizes of the runs before it (every run's CSR length is a multiple of 8)
+    struct Off {
+        size_t t, e, c, s, r, v;
+    };
+    std::vector<Off> off((size_t)T + 1, Off{0, 0, 0, 0, 0, 0});
+    for (int t = 0; t < T; t++) {
+        const TileSet& p = part[(size_t)t];
+        const Off& a = off[(size_t)t];
+        off[(size_t)t + 1] = Off{a.t + p.tiles.size(), a.e + p.ent.size(), a.c + p.csr.size(),
+                                 a.s + p.segs.size(), a.r + p.rows.size(), a.v + p.val64.size()};
+    }
+    const Off& all = off[(size_t)T];
+    out.tiles.resize(all.t);
+    out.ent.resize(all.e);
+    out.csr.resize(all.c);
+    out.segs.resize(all.s);
+    out.rows.resize(all.r);
+    out.val64.resize(all.v);
+    auto place = [&](int t) {
+        TileSet& p = part[(size_t)t];
+        const Off& a = off[(size_t)t];
+        for (size_t i = 0; i < p.tiles.size(); i++) {
+            TileHdr h = p.tiles[i];
+            h.eoff += (long long)a.e;
+            h.roff += (long long)a.r;
+            h.soff += (long long)a.s;
+            h.coff += (long long)a.c;
+            out.tiles[a.t + i] = h;
+        }
+        std::copy(p.ent.begin(), p.ent.end(), out.ent.begin() + (long long)a.e);
+        std::copy(p.csr.begin(), p.csr.end(), out.csr.begin() + (long long)a.c);
+        std::copy(p.segs.begin(), p.segs.end(), out.segs.begin() + (long long)a.s);
+        std::copy(p.rows.begin(), p.rows.end(), out.rows.begin() + (long long)a.r);
+        std::copy(p.val64.begin(), p.val64.end(), out.val64.begin() + (long long)a.v);
+        p = TileSet();
+    };
+    pool.clear();
+    for (int t = 1; t < T; t++)
+        pool.emplace_back(place, t);
+    place(0);
+    for (auto& th : pool)
+        th.join();
 }
 
 }  // namespace btc
