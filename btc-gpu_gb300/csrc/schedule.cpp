@@ -146,7 +146,8 @@ btc_status blocking(const int32_t* xyz, int64_t n, int I, int J, int K, int bs, 
     // since the snapshot is descended further, and a change of a global level
     // (which changes every bucket code) re-routes from the root.
     const int64_t CH = 1 << 16;
-    std::vector<int> leaf((size_t)std::min<int64_t>(n, CH));
+    // leaf_block: the block each entry's snapshot leaf held, for prefetching
+    std::vector<int> leaf((size_t)std::min<int64_t>(n, CH)), leaf_block((size_t)std::min<int64_t>(n, CH));
     std::vector<int64_t> codes((size_t)std::min<int64_t>(n, CH) * 3);
     std::atomic<int> bad(0);
     for (int64_t base = 0; base < n; base += CH) {
@@ -163,6 +164,7 @@ btc_status blocking(const int32_t* xyz, int64_t n, int I, int J, int K, int bs, 
                             return;
                         }
                     leaf[(size_t)k] = route(nodes, 0, pc, g0);
+                    leaf_block[(size_t)k] = nodes[(size_t)leaf[(size_t)k]].block;
                 }
             };
             const int nt = std::max(1, std::min<int>(threads, (int)(cn / 4096) + 1));
@@ -176,6 +178,16 @@ btc_status blocking(const int32_t* xyz, int64_t n, int I, int J, int K, int bs, 
                 return BTC_ERR_RANGE;
         }
       for (int64_t k = 0; k < cn; k++) {
+        // The appends land in scattered blocks: fetch ahead the record of the
+        // block an entry 16 further was routed to and the tail of the entry
+        // list 8 further (hints only; a block split since the snapshot
+        // merely wastes the fetch).
+        if (k + 16 < cn)
+            __builtin_prefetch(&blocks[(size_t)leaf_block[(size_t)(k + 16)]]);
+        if (k + 8 < cn) {
+            const BlockRec& F = blocks[(size_t)leaf_block[(size_t)(k + 8)]];
+            __builtin_prefetch(F.ent.data() + F.ent.size(), 1);
+        }
         const int64_t i = base + k;
         const int32_t* p = xyz + 3 * i;
         int64_t pc[3];
@@ -247,7 +259,12 @@ btc_status blocking(const int32_t* xyz, int64_t n, int I, int J, int K, int bs, 
             B.code[a] = B.code[a] << 1;
             t1.clear();
             t2.clear();
-            for (int32_t e : B.ent) {
+            // a split re-buckets the block's entries: their coordinates lie
+            // scattered over the whole input, so they are fetched ahead
+            for (size_t j = 0; j < B.ent.size(); j++) {
+                if (j + 16 < B.ent.size())
+                    __builtin_prefetch(xyz + 3 * (int64_t)B.ent[j + 16] + a);
+                const int32_t e = B.ent[j];
                 int64_t hv;
                 if (!ax[a].hx(g[a], xyz[3 * (int64_t)e + a], hv))
                     return BTC_ERR_RANGE;
