@@ -4,7 +4,8 @@
 // starts with '#' or '%', or does not begin with three integers and a number
 // (stream extraction semantics: leading whitespace skipped, extra fields
 // ignored); coord_base is subtracted and out-of-range coordinates are an
-// error.  The whole file is read at once and parsed without iostreams.
+// error.  The whole file is read at once and parsed without iostreams, in
+// newline-aligned chunks on host threads for large files.
 #include <algorithm>
 #include <atomic>
 #include <cerrno>
@@ -189,41 +190,77 @@ btc_status btc_read_entries(const char* path, int32_t coord_base, int32_t I, int
         return BTC_ERR_IO;
     }
     std::fclose(f);
-    std::vector<int32_t> cx;
-    std::vector<double> cv;
-    cx.reserve((size_t)(size / 16) * 3);
-    cv.reserve((size_t)(size / 16));
-    const char* p = buf.data();
-    const char* end = p + buf.size();
-    int64_t ln = 0;
-    while (p < end) {
-        const char* eol = (const char*)std::memchr(p, '\n', (size_t)(end - p));
-        if (!eol)
-            eol = end;
-        ln++;
-        const char* q = p;
-        if (q < eol && *q != '#' && *q != '%') {
-            int32_t x, y, z;
-            double v;
-            if (parse_int(q, eol, x) && parse_int(q, eol, y) && parse_int(q, eol, z) &&
-                parse_double(q, eol, v)) {
-                x -= coord_base;
-                y -= coord_base;
-                z -= coord_base;
-                if (x < 0 || x >= I || y < 0 || y >= J || z < 0 || z >= K) {
-                    if (line_no)
-                        *line_no = ln;
-                    return BTC_ERR_RANGE;
-                }
-                cx.push_back(x);
-                cx.push_back(y);
-                cx.push_back(z);
-                cv.push_back(v);
-            }
-        }
-        p = eol + 1;
+    // Lines are parsed in chunks cut at newlines, one per thread; a chunk
+    // stops at its first out-of-range line, the earliest such line in file
+    // order is the error (as the serial scan would report it), and the
+    // chunks' entries are concatenated in order.
+    const char* begin = buf.data();
+    const char* end = begin + buf.size();
+    int T = size >= (64LL << 20) ? (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency())) : 1;
+    std::vector<const char*> cut((size_t)T + 1, end);
+    cut[0] = begin;
+    for (int t = 1; t < T; t++) {
+        const char* c = std::max(begin + (size_t)((long long)buf.size() * t / T), cut[(size_t)t - 1]);
+        const char* nl = c < end ? (const char*)std::memchr(c, '\n', (size_t)(end - c)) : nullptr;
+        cut[(size_t)t] = nl ? nl + 1 : end;
     }
-    int64_t cnt = (int64_t)cv.size();
+    struct Part {
+        std::vector<int32_t> cx;
+        std::vector<double> cv;
+        int64_t lines = 0, bad = 0;  // lines in the chunk; 1-based line of its first error, 0 if none
+    };
+    std::vector<Part> part((size_t)T);
+    auto work = [&](int t) {
+        Part& P = part[(size_t)t];
+        const char* p = cut[(size_t)t];
+        const char* e = cut[(size_t)t + 1];
+        P.cx.reserve((size_t)((e - p) / 16) * 3);
+        P.cv.reserve((size_t)((e - p) / 16));
+        while (p < e) {
+            const char* eol = (const char*)std::memchr(p, '\n', (size_t)(e - p));
+            if (!eol)
+                eol = e;
+            P.lines++;
+            const char* q = p;
+            if (q < eol && *q != '#' && *q != '%') {
+                int32_t x, y, z;
+                double v;
+                if (parse_int(q, eol, x) && parse_int(q, eol, y) && parse_int(q, eol, z) &&
+                    parse_double(q, eol, v)) {
+                    x -= coord_base;
+                    y -= coord_base;
+                    z -= coord_base;
+                    if (x < 0 || x >= I || y < 0 || y >= J || z < 0 || z >= K) {
+                        P.bad = P.lines;
+                        return;
+                    }
+                    P.cx.push_back(x);
+                    P.cx.push_back(y);
+                    P.cx.push_back(z);
+                    P.cv.push_back(v);
+                }
+            }
+            p = eol + 1;
+        }
+    };
+    {
+        std::vector<std::thread> pool;
+        for (int t = 1; t < T; t++)
+            pool.emplace_back(work, t);
+        work(0);
+        for (auto& th : pool)
+            th.join();
+    }
+    int64_t ln = 0, cnt = 0;
+    for (const Part& P : part) {
+        if (P.bad) {
+            if (line_no)
+                *line_no = ln + P.bad;
+            return BTC_ERR_RANGE;
+        }
+        ln += P.lines;
+        cnt += (int64_t)P.cv.size();
+    }
     *xyz = (int32_t*)std::malloc(sizeof(int32_t) * 3 * (size_t)std::max<int64_t>(cnt, 1));
     *val = (double*)std::malloc(sizeof(double) * (size_t)std::max<int64_t>(cnt, 1));
     if (!*xyz || !*val) {
@@ -233,8 +270,14 @@ btc_status btc_read_entries(const char* path, int32_t coord_base, int32_t I, int
         *val = nullptr;
         return BTC_ERR_ALLOC;
     }
-    std::memcpy(*xyz, cx.data(), sizeof(int32_t) * 3 * (size_t)cnt);
-    std::memcpy(*val, cv.data(), sizeof(double) * (size_t)cnt);
+    int64_t o = 0;
+    for (const Part& P : part) {
+        if (!P.cv.empty()) {
+            std::memcpy(*xyz + 3 * o, P.cx.data(), sizeof(int32_t) * P.cx.size());
+            std::memcpy(*val + o, P.cv.data(), sizeof(double) * P.cv.size());
+        }
+        o += (int64_t)P.cv.size();
+    }
     *n = cnt;
     return BTC_OK;
 }

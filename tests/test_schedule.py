@@ -122,6 +122,38 @@ def test_reader_skips_like_the_reference(tmp_path):
     assert val.tolist() == [0.5, 0.7, -2.25, 0.0]
 
 
+_TRICKY = ("# comment\n% also\n\n1 2 3 0.5\n4 5 6 7e-1 extra fields\n1.5 2 3 4\nbad line\n"
+           "  7 8 9   -2.25\n1 2\n3 3 3 inf\n2 2 2 1e\n2 2 2 1e999\n5 5 5 1e-999\n")
+
+
+def test_reader_large_file_parses_like_small_ones(tmp_path):
+    """Files of 64 MB and more are parsed in newline-aligned chunks on host
+    threads: the entries, their order and the skipped lines are the same as
+    for the small file repeated."""
+    reps = (64 << 20) // len(_TRICKY) + 1000
+    p = tmp_path / "big.train"
+    p.write_text(_TRICKY * reps)
+    xyz, val = bg.read_entries(str(p), 1, 10, 10, 10)
+    one_xyz = np.array([[0, 1, 2], [3, 4, 5], [6, 7, 8], [4, 4, 4]], np.int32)
+    one_val = np.array([0.5, 0.7, -2.25, 0.0])
+    assert xyz.shape == (4 * reps, 3)
+    assert np.array_equal(xyz, np.tile(one_xyz, (reps, 1))) and np.array_equal(val, np.tile(one_val, reps))
+
+
+def test_reader_large_file_reports_the_first_bad_line(tmp_path):
+    """An out-of-range line late in a chunked file is reported by its line
+    number in the whole file, the first such line winning."""
+    reps = (64 << 20) // len(_TRICKY) + 1000
+    lines_per = _TRICKY.count("\n")
+    k1, k2 = reps * 3 // 4, reps - 5
+    text = _TRICKY * k1 + "11 1 1 1.0\n" + _TRICKY * (k2 - k1) + "1 11 1 1.0\n" + _TRICKY * (reps - k2)
+    p = tmp_path / "bad.train"
+    p.write_text(text)
+    with pytest.raises(bg.BtcError) as e:
+        bg.read_entries(str(p), 1, 10, 10, 10)
+    assert e.value.status == 8 and e.value.line == k1 * lines_per + 1
+
+
 def test_reader_rejects_out_of_range(tmp_path):
     p = tmp_path / "t.train"
     p.write_text("1 1 1 1.0\n0 1 1 2.0\n")
