@@ -20,6 +20,9 @@
 //   --init-file FILE           initial factors as raw doubles A[I*r], B[J*r], C[K*r]
 //   --dump-factors DIR         write A.txt, B.txt, C.txt (rows of %.17g)
 //   --device N                 CUDA device ordinal
+//   --bin-cache DIR            keep parsed train/test files as binary caches
+//                              in DIR (<file name>.btcbin) and read them
+//                              instead of the text while they match
 #include <sys/stat.h>
 
 #include <cerrno>
@@ -48,7 +51,7 @@ namespace {
 btc_config cfg;
 string dataset_name = "tensor";
 string output_root = "output";
-string precision = "f32", mode_name = "hogwild", dump_dir, init_file;
+string precision = "f32", mode_name = "hogwild", dump_dir, init_file, bin_cache_dir;
 bool have_seed = false;
 unsigned long long seed = 0;
 double init_lo = 0.02, init_hi = 0.1;
@@ -93,6 +96,7 @@ void print_usage(const char* program)
     cerr << "  --init-file FILE              Initial factors (raw doubles A, B, C)" << endl;
     cerr << "  --dump-factors DIR            Write the final factors as text" << endl;
     cerr << "  --device N                    CUDA device. Default: 0" << endl;
+    cerr << "  --bin-cache DIR               Binary caches of the parsed input files" << endl;
 }
 
 bool read_option_value(const string& arg, int& index, int argc, char** argv, string& option, string& value)
@@ -148,6 +152,8 @@ bool apply_option(const string& o, const string& v)
         init_file = v;
     else if (o == "--device")
         cfg.device = atoi(v.c_str());
+    else if (o == "--bin-cache")
+        bin_cache_dir = v;
     else {
         cerr << "Unknown option: " << o << endl;
         return false;
@@ -258,8 +264,19 @@ void read_entries(const std::vector<string>& cands, const string& label, int coo
         exit(1);
     }
     int64_t line = 0;
-    btc_status st = btc_read_entries(opened.c_str(), coord_base, cfg.I, cfg.J, cfg.K, &out.xyz, &out.val,
-                                     &out.n, &line);
+    btc_status st;
+    if (bin_cache_dir.empty()) {
+        st = btc_read_entries(opened.c_str(), coord_base, cfg.I, cfg.J, cfg.K, &out.xyz, &out.val, &out.n, &line);
+    } else {
+        const size_t slash = opened.find_last_of('/');
+        const string cache = join_path(bin_cache_dir, opened.substr(slash == string::npos ? 0 : slash + 1) + ".btcbin");
+        int32_t from_cache = 0;
+        st = btc_read_entries_cached(opened.c_str(), cache.c_str(), coord_base, cfg.I, cfg.J, cfg.K, &out.xyz,
+                                     &out.val, &out.n, &line, &from_cache);
+        if (st == BTC_OK)
+            cerr << (from_cache ? "Read " : "Parsed the text; refreshed (where writable) ") << label
+                 << " binary cache " << cache << endl;
+    }
     if (st == BTC_ERR_RANGE) {
         std::ifstream f(opened.c_str());
         string s;

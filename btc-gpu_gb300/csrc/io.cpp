@@ -15,8 +15,12 @@
 #include <cstdlib>
 #include <cstring>
 #include <random>
+#include <string>
 #include <thread>
 #include <vector>
+
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include "btc_gpu.h"
 #include "common.h"
@@ -280,6 +284,109 @@ btc_status btc_read_entries(const char* path, int32_t coord_base, int32_t I, int
     }
     *n = cnt;
     return BTC_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Binary cache of a parsed file: this header, then n x 3 int32 coordinates
+// (base already subtracted) and n doubles, in host byte order.
+struct CacheHdr {
+    char magic[8];
+    int32_t coord_base, I, J, K;
+    int64_t n, src_size, src_mtime_ns;
+};
+constexpr char kCacheMagic[8] = {'B', 'T', 'C', 'C', 'O', 'O', '0', '1'};
+
+bool source_stamp(const char* path, int64_t& size, int64_t& mtime_ns)
+{
+    struct stat st;
+    if (stat(path, &st) != 0)
+        return false;
+    size = (int64_t)st.st_size;
+    mtime_ns = (int64_t)st.st_mtim.tv_sec * 1000000000LL + (int64_t)st.st_mtim.tv_nsec;
+    return true;
+}
+
+bool read_cache(const char* cache, const CacheHdr& want, int32_t** xyz, double** val, int64_t* n)
+{
+    FILE* f = std::fopen(cache, "rb");
+    if (!f)
+        return false;
+    CacheHdr h;
+    bool ok = std::fread(&h, sizeof h, 1, f) == 1 && std::memcmp(h.magic, kCacheMagic, 8) == 0 &&
+              h.coord_base == want.coord_base && h.I == want.I && h.J == want.J && h.K == want.K &&
+              h.src_size == want.src_size && h.src_mtime_ns == want.src_mtime_ns && h.n >= 0;
+    if (ok) {
+        struct stat st;
+        ok = fstat(fileno(f), &st) == 0 &&
+             (int64_t)st.st_size == (int64_t)sizeof h + h.n * (int64_t)(3 * sizeof(int32_t) + sizeof(double));
+    }
+    int32_t* x = nullptr;
+    double* v = nullptr;
+    if (ok) {
+        x = (int32_t*)std::malloc(sizeof(int32_t) * 3 * (size_t)std::max<int64_t>(h.n, 1));
+        v = (double*)std::malloc(sizeof(double) * (size_t)std::max<int64_t>(h.n, 1));
+        ok = x && v && std::fread(x, sizeof(int32_t) * 3, (size_t)h.n, f) == (size_t)h.n &&
+             std::fread(v, sizeof(double), (size_t)h.n, f) == (size_t)h.n;
+    }
+    std::fclose(f);
+    if (!ok) {
+        std::free(x);
+        std::free(v);
+        return false;
+    }
+    *xyz = x;
+    *val = v;
+    *n = h.n;
+    return true;
+}
+
+void write_cache(const char* cache, const CacheHdr& hdr, const int32_t* xyz, const double* val)
+{
+    std::string tmp = std::string(cache) + ".tmp." + std::to_string((long long)getpid());
+    FILE* f = std::fopen(tmp.c_str(), "wb");
+    if (!f)
+        return;  // the cache is an optimisation: an unwritable location is no error
+    bool ok = std::fwrite(&hdr, sizeof hdr, 1, f) == 1 &&
+              std::fwrite(xyz, sizeof(int32_t) * 3, (size_t)hdr.n, f) == (size_t)hdr.n &&
+              std::fwrite(val, sizeof(double), (size_t)hdr.n, f) == (size_t)hdr.n;
+    ok = std::fclose(f) == 0 && ok;
+    if (!ok || std::rename(tmp.c_str(), cache) != 0)
+        std::remove(tmp.c_str());
+}
+
+}  // namespace
+
+extern "C" {
+
+btc_status btc_read_entries_cached(const char* path, const char* cache, int32_t coord_base, int32_t I, int32_t J,
+                                   int32_t K, int32_t** xyz, double** val, int64_t* n, int64_t* line_no,
+                                   int32_t* from_cache)
+{
+    if (!path || !cache || !xyz || !val || !n || !from_cache)
+        return BTC_ERR_ARG;
+    *from_cache = 0;
+    CacheHdr hdr{};
+    std::memcpy(hdr.magic, kCacheMagic, 8);
+    hdr.coord_base = coord_base;
+    hdr.I = I;
+    hdr.J = J;
+    hdr.K = K;
+    const bool stamped = source_stamp(path, hdr.src_size, hdr.src_mtime_ns);
+    if (stamped && read_cache(cache, hdr, xyz, val, n)) {
+        if (line_no)
+            *line_no = 0;
+        *from_cache = 1;
+        return BTC_OK;
+    }
+    btc_status st = btc_read_entries(path, coord_base, I, J, K, xyz, val, n, line_no);
+    if (st == BTC_OK && stamped) {
+        hdr.n = *n;
+        write_cache(cache, hdr, *xyz, *val);
+    }
+    return st;
 }
 
 btc_status btc_shuffle_entries(int32_t* xyz, double* val, int64_t n, uint32_t seed)

@@ -82,6 +82,8 @@ SIGNATURES = {
     "btc_config_default": ([P], ctypes.c_int),
     "btc_config_validate": ([P], ctypes.c_int),
     "btc_read_entries": ([ctypes.c_char_p, I32, I32, I32, I32, P, P, P, P], ctypes.c_int),
+    "btc_read_entries_cached": ([ctypes.c_char_p, ctypes.c_char_p, I32, I32, I32, I32, P, P, P, P, P],
+                                ctypes.c_int),
     "btc_free": ([P], None),
     "btc_shuffle_entries": ([P, P, I64, U32], ctypes.c_int),
     "btc_schedule_build": ([P, P, I64, P], ctypes.c_int),
@@ -178,12 +180,22 @@ def shuffle(xyz, val, seed=42):
     return xyz, val
 
 
-def read_entries(path, coord_base, I, J, K):
+def read_entries(path, coord_base, I, J, K, cache=None):
+    """Entries of a text file as (xyz int32 [n, 3], val float64 [n]).  With
+    `cache`, through btc_read_entries_cached; the returned arrays are the same
+    and `read_entries.from_cache` tells whether the cache was used."""
     L = _lib()
     px, pv = ctypes.c_void_p(), ctypes.c_void_p()
     n, line = ctypes.c_int64(), ctypes.c_int64()
-    st = L.btc_read_entries(path.encode(), coord_base, I, J, K, ctypes.byref(px), ctypes.byref(pv),
-                            ctypes.byref(n), ctypes.byref(line))
+    if cache is None:
+        st = L.btc_read_entries(path.encode(), coord_base, I, J, K, ctypes.byref(px), ctypes.byref(pv),
+                                ctypes.byref(n), ctypes.byref(line))
+        read_entries.from_cache = False
+    else:
+        fc = ctypes.c_int32()
+        st = L.btc_read_entries_cached(path.encode(), cache.encode(), coord_base, I, J, K, ctypes.byref(px),
+                                       ctypes.byref(pv), ctypes.byref(n), ctypes.byref(line), ctypes.byref(fc))
+        read_entries.from_cache = bool(fc.value)
     if st != 0:
         err = BtcError(st, "btc_read_entries")
         err.line = line.value

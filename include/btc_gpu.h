@@ -142,6 +142,17 @@ btc_status btc_read_entries(const char *path, int32_t coord_base, int32_t I, int
                             int32_t K, int32_t **xyz, double **val, int64_t *n,
                             int64_t *line_no);
 void btc_free(void *p);
+/* btc_read_entries through a binary cache (no reference counterpart): when
+ * the file at `cache` was written for this source file (same size and
+ * modification time) and the same coord_base, I, J, K, its entries are read
+ * as they are; otherwise `path` is parsed with btc_read_entries and, on
+ * success, the cache is written (atomically; an unwritable location is no
+ * error).  The cache holds a 48-byte header, then n x 3 int32 coordinates
+ * (base subtracted) and n doubles in host byte order.  *from_cache is 1 when
+ * the entries came from the cache. */
+btc_status btc_read_entries_cached(const char *path, const char *cache, int32_t coord_base,
+                                   int32_t I, int32_t J, int32_t K, int32_t **xyz, double **val,
+                                   int64_t *n, int64_t *line_no, int32_t *from_cache);
 /* std::shuffle with std::mt19937(seed) over n entries, as main.cpp:303-306
  * does with seed 42; permutes xyz and val together. */
 btc_status btc_shuffle_entries(int32_t *xyz, double *val, int64_t n, uint32_t seed);

@@ -72,7 +72,7 @@ def test_groups_slots_coe_match_reference(built):
     (15, (2000, 2000, 2000), 100_000, (1.5, 1.5, 1.5), 64),
 ])
 def test_strata_and_groups_match_oracle_on_skewed_inputs(seed, dims, nnz, zipf, block_s):
-    """The product builder (indexed first-fit strata, threaded padding) gives
+    """The product builder (threaded first-fit strata, threaded padding) gives
     the oracle's strata, groups and coe weights on larger skewed inputs than
     the fixtures: hot rows make long chains of mutually conflicting blocks."""
     import oracle
@@ -154,6 +154,36 @@ def test_reader_large_file_reports_the_first_bad_line(tmp_path):
     assert e.value.status == 8 and e.value.line == k1 * lines_per + 1
 
 
+def test_binary_cache_round_trip_and_invalidation(tmp_path):
+    p = tmp_path / "t.train"
+    p.write_text(_TRICKY)
+    cache = str(tmp_path / "t.train.btcbin")
+    want = bg.read_entries(str(p), 1, 10, 10, 10)
+    got = bg.read_entries(str(p), 1, 10, 10, 10, cache=cache)  # parses, writes the cache
+    assert not bg.read_entries.from_cache and os.path.exists(cache)
+    again = bg.read_entries(str(p), 1, 10, 10, 10, cache=cache)
+    assert bg.read_entries.from_cache
+    for a, b, c in zip(want, got, again):
+        assert np.array_equal(a, b) and np.array_equal(a, c) and a.dtype == c.dtype
+    # another base or shape is not served from this cache (and rewrites it)
+    bg.read_entries(str(p), 0, 11, 11, 11, cache=cache)
+    assert not bg.read_entries.from_cache
+    bg.read_entries(str(p), 1, 10, 10, 10, cache=cache)
+    assert not bg.read_entries.from_cache
+    # an edited source is parsed again
+    p.write_text(_TRICKY + "9 9 9 1.25\n")
+    x2, v2 = bg.read_entries(str(p), 1, 10, 10, 10, cache=cache)
+    assert not bg.read_entries.from_cache and v2[-1] == 1.25 and len(v2) == len(want[1]) + 1
+    # a truncated cache falls back to the text
+    with open(cache, "r+b") as f:
+        f.truncate(60)
+    x3, v3 = bg.read_entries(str(p), 1, 10, 10, 10, cache=cache)
+    assert not bg.read_entries.from_cache and np.array_equal(v3, v2)
+    # an unwritable cache location is no error
+    x4, v4 = bg.read_entries(str(p), 1, 10, 10, 10, cache=str(tmp_path / "missing" / "c.btcbin"))
+    assert np.array_equal(v4, v2)
+
+
 def test_reader_rejects_out_of_range(tmp_path):
     p = tmp_path / "t.train"
     p.write_text("1 1 1 1.0\n0 1 1 2.0\n")
@@ -210,3 +240,7 @@ def test_cli_arguments_like_the_reference():
     assert r.returncode == 1 and "Unknown option: --bogus" in r.stderr
     r = subprocess.run([cli, "ds", "10", "10", "10", "/tmp", "2"], capture_output=True, text=True)
     assert r.returncode == 1 and "coord_base must be 0 or 1." in r.stderr
+    # this library's own options are accepted next to the reference's
+    r = subprocess.run([cli, "ds", "10", "10", "10", "/tmp", "0", "/tmp", "--rank", "101", "--bin-cache", "/tmp",
+                        "--precision", "bf16", "--mode", "staged"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Unknown option" not in r.stderr and "rank r must be in [1, 100]" in r.stderr
