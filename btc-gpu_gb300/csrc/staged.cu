@@ -10,6 +10,7 @@
 //   3. owners  one lane group per owner segment (a run of <= seg entries
 //              sharing a row of one mode) sums err * (other two rows) from S
 //              in registers and adds coe*lr*(sum - count*reg*row) to the row
+//              (row: the snapshot; for a FAST row, its value at write time)
 //              in global memory with one vector atomic per 16 bytes (BF16
 //              rows without a master: the stochastically rounded difference
 //              to the snapshot, by bf16x2 atomic adds), so a row is written
