@@ -108,14 +108,17 @@ void finish_block_codes(BlockRec& b)
 
 // Route one entry from `node` down to a leaf with bucket codes pc at global
 // levels g (search_block, block.cu:64-88).
+// The left child of a node split on axis a has len[a] + 1 and code[a] << 1
+// (Create_Btree below), so each step reads the parent only.
 inline int route(const std::vector<Node>& nodes, int node, const int64_t* pc, const int* g)
 {
-    while (nodes[node].left >= 0) {
-        const int a = axis_of_h(nodes[node].h);
-        const Node& lc = nodes[nodes[node].left];
-        node = prefix_bits(pc[a], g[a], lc.len[a]) == lc.code[a] ? nodes[node].left : nodes[node].right;
+    for (;;) {
+        const Node& P = nodes[(size_t)node];
+        if (P.left < 0)
+            return node;
+        const int a = axis_of_h(P.h);
+        node = prefix_bits(pc[a], g[a], P.len[a] + 1) == (P.code[a] << 1) ? P.left : P.right;
     }
-    return node;
 }
 
 btc_status blocking(const int32_t* xyz, int64_t n, int I, int J, int K, int bs, int threads, Schedule& s)
