@@ -34,6 +34,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -94,7 +95,7 @@ class Clocks:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+        self.path = os.path.join(tempfile.gettempdir(), "btc_bench_clocks_%d.csv" % os.getpid())
 
     def start(self):
         try:

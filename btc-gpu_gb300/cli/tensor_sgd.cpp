@@ -66,6 +66,26 @@ string join_path(const string& dir, const string& name)
     return dir + "/" + name;
 }
 
+// mkdir -p without a shell: every prefix of `path` that ends at a '/' is
+// created with mkdir(2) (existing directories are fine), so no character of
+// the path is ever interpreted as a command.
+bool make_dirs(const string& path)
+{
+    if (path.empty())
+        return true;
+    for (size_t i = 1; i <= path.size(); i++) {
+        if (i < path.size() && path[i] != '/')
+            continue;
+        const string part = path.substr(0, i);
+        if (part.empty() || part == "/")
+            continue;
+        if (mkdir(part.c_str(), 0777) != 0 && errno != EEXIST)
+            return false;
+    }
+    struct stat st;
+    return stat(path.c_str(), &st) == 0 && S_ISDIR(st.st_mode);
+}
+
 void print_usage(const char* program)
 {
     cerr << "Usage: " << program << " <dataset> <I> <J> <K> [data_dir] [coord_base] [output_dir] [options]" << endl;
@@ -453,11 +473,8 @@ int main(int argc, char** argv)
     if (!dir.empty() && dir[dir.size() - 1] != '/' && dir[dir.size() - 1] != '\\')
         dir += "/";
     dir += dataset_name + "_" + rs.str() + "/";
-    {
-        string cmd = "mkdir -p \"" + dir + "\"";
-        if (system(cmd.c_str()) != 0)
-            cerr << "mkdir failed for " << dir << endl;
-    }
+    if (!make_dirs(dir))
+        cerr << "mkdir failed for " << dir << endl;
     string report = dir + "block_parallel.txt";
     if (btc_schedule_write_report(sched, &cfg, report.c_str()) != BTC_OK)
         cerr << "Failed to open " << report << endl;
@@ -504,7 +521,8 @@ int main(int argc, char** argv)
         if ((st = btc_train_epoch(ctx, &es)))
             fail(st, "warm-up epoch");
         for (int m = 0; m < 3; m++)
-            btc_ctx_set_factors(ctx, m, F[m].data());
+            if ((st = btc_ctx_set_factors(ctx, m, F[m].data())))
+                fail(st, "factor restore after warm-up");
         double prev = 0;
         int have_prev = 0;
         for (int epoch = 0; epoch < cfg.epochs; epoch++) {
@@ -543,8 +561,7 @@ int main(int argc, char** argv)
         printf("first train entry: (%d,%d,%d) ref=%f pred=%f\n", e[0], e[1], e[2], train.val[0], pred);
     }
     if (!dump_dir.empty()) {
-        string cmd = "mkdir -p \"" + dump_dir + "\"";
-        if (system(cmd.c_str()) != 0)
+        if (!make_dirs(dump_dir))
             cerr << "mkdir failed for " << dump_dir << endl;
         const char* names[3] = {"A.txt", "B.txt", "C.txt"};
         for (int m = 0; m < 3; m++)

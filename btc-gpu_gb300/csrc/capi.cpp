@@ -131,6 +131,33 @@ int resident_blocks(const btc_config& c)
     return p.multiProcessorCount * per;
 }
 
+// Whether every (x, y, z) of n entries lies in [0,I) x [0,J) x [0,K); large
+// inputs are checked on host threads.
+bool coords_in_range(const int32_t* xyz, int64_t n, int32_t I, int32_t J, int32_t K, int threads)
+{
+    if (n <= 0)
+        return true;
+    const int T = n >= (1LL << 22) ? std::max(1, std::min(threads, 32)) : 1;
+    std::vector<char> ok((size_t)T, 1);
+    auto work = [&](int t) {
+        const int64_t lo = n * t / T, hi = n * (t + 1) / T;
+        for (int64_t i = lo; i < hi; i++) {
+            const int32_t* c = xyz + 3 * i;
+            if ((uint32_t)c[0] >= (uint32_t)I || (uint32_t)c[1] >= (uint32_t)J || (uint32_t)c[2] >= (uint32_t)K) {
+                ok[(size_t)t] = 0;
+                return;
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < T; t++)
+        pool.emplace_back(work, t);
+    work(0);
+    for (auto& th : pool)
+        th.join();
+    return std::all_of(ok.begin(), ok.end(), [](char v) { return v != 0; });
+}
+
 template <typename T>
 void free_dev(T*& p)
 {
@@ -735,6 +762,11 @@ btc_status btc_ctx_create(const btc_config* cfg, const btc_schedule* s, const in
         return rc;
     if (s->s.train_nnz != ntr || s->s.I != cfg->I || s->s.J != cfg->J || s->s.K != cfg->K)
         return BTC_ERR_ARG;
+    // every coordinate the kernels will use as a row index must name a row:
+    // an out-of-range train or test entry would read or write past a factor
+    if (!coords_in_range(txyz, ntr, cfg->I, cfg->J, cfg->K, default_threads(*cfg)) ||
+        !coords_in_range(sxyz, nte, cfg->I, cfg->J, cfg->K, default_threads(*cfg)))
+        return BTC_ERR_RANGE;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
         cudaGetLastError();

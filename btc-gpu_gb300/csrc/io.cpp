@@ -330,6 +330,12 @@ bool read_cache(const char* cache, const CacheHdr& want, int32_t** xyz, double**
         v = (double*)std::malloc(sizeof(double) * (size_t)std::max<int64_t>(h.n, 1));
         ok = x && v && std::fread(x, sizeof(int32_t) * 3, (size_t)h.n, f) == (size_t)h.n &&
              std::fread(v, sizeof(double), (size_t)h.n, f) == (size_t)h.n;
+        // the header cannot vouch for the payload (a damaged or edited file,
+        // a stamp collision): coordinates are held to the ranges the text
+        // parser enforces, and a cache that breaks them is parsed again
+        for (int64_t i = 0; ok && i < h.n; i++)
+            ok = (uint32_t)x[3 * i] < (uint32_t)want.I && (uint32_t)x[3 * i + 1] < (uint32_t)want.J &&
+                 (uint32_t)x[3 * i + 2] < (uint32_t)want.K;
     }
     std::fclose(f);
     if (!ok) {

@@ -1,10 +1,10 @@
 // btc_eval_sums_noalloc: the FP64 error sums of compute_metrics_gpu for
 // callers that cannot allocate device memory.
 //
-// Some callers of this library cannot call cudaMalloc: code that runs while
-// a stream is being captured into a CUDA graph (an allocation there fails
-// or breaks the capture), code embedded in a host framework that owns every
-// device allocation through its own pool, and latency-critical loops that
+// Some callers of this library cannot call cudaMalloc: code embedded in a
+// host framework that owns every device allocation through its own pool (a
+// caching allocator that has already reserved the memory, an engine that
+// forbids allocation once it has started), and latency-critical loops that
 // must not take the driver's allocation lock.  This entry point serves them:
 // the caller passes device pointers for the inputs and for the three output
 // sums, and the only scratch the reduction needs -- one partial triple per

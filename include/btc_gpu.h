@@ -179,7 +179,9 @@ btc_status btc_schedule_write_report(const btc_schedule *s, const btc_config *cf
                                      const char *path);
 void btc_schedule_free(btc_schedule *s);
 
-/* ---- device context (replaces sgd_train's state, sgd_Kernel.cu:1042-1266) */
+/* ---- device context (replaces sgd_train's state, sgd_Kernel.cu:1042-1266)
+ * Every train and test coordinate must lie in [0,I) x [0,J) x [0,K):
+ * otherwise BTC_ERR_RANGE, before anything reaches the device. */
 btc_status btc_ctx_create(const btc_config *cfg, const btc_schedule *s, const int32_t *train_xyz,
                           const double *train_val, int64_t ntrain, const int32_t *test_xyz,
                           const double *test_val, int64_t ntest, btc_ctx **out);
@@ -301,13 +303,16 @@ btc_status btc_device_info(int32_t device, char *name, int32_t *sm_count, int64_
 
 /* ---- error sums without allocation ----------------------------------------
  * No counterpart in the reference: an added entry point for callers that
- * cannot call cudaMalloc -- code running during CUDA graph capture, hosts
- * whose framework owns every device allocation, allocation-free real-time
- * loops.  It computes the FP64 sums (SSE, SAE, sum ref^2) of
- * compute_metrics_gpu over n entries and writes them to sums[0..2].
+ * cannot call cudaMalloc -- hosts whose framework owns every device
+ * allocation (a caching allocator that has reserved the memory, an engine
+ * that forbids allocation after start-up), allocation-free real-time loops.
+ * It computes the FP64 sums (SSE, SAE, sum ref^2) of compute_metrics_gpu
+ * over n entries and writes them to sums[0..2].
  * Every pointer is DEVICE memory supplied by the caller: xyz is n x 3 int32,
  * val n doubles, A/B/C row-major factors of `dtype` (F32 or F64) with
- * `row_stride` elements per row (>= rank), sums 3 doubles.  The launch goes
+ * `row_stride` elements per row (>= rank), sums 3 doubles.  Every entry's
+ * x, y and z must name an existing row of A, B and C respectively: the
+ * call is given no row counts and checks none.  The launch goes
  * on `stream` (a cudaStream_t, NULL for the default stream) and is not
  * waited for.
  * Its only scratch is a file-scope device array of BTC_NOALLOC_MAX_ENTRIES /

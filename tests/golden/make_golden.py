@@ -102,7 +102,7 @@ def make_case(name, ref_bin, seed):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("BTC_REFERENCE_SRC", "/root/reference")
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", "REF=" + ref])
     ref_bin = os.path.join(ROOT, "oracle", "_ref", "ref_block")
     for i, name in enumerate(sorted(CASES)):

@@ -52,3 +52,34 @@ def test_cli_runs_like_the_reference(tmp_path, extra):
         assert os.path.getsize(os.path.join(d, name)) > 0
     A = np.loadtxt(tmp_path / "f" / "A.txt")
     assert A.shape == (I, 16) and np.isfinite(A).all()
+
+
+def test_cli_early_stop_and_literal_output_directory(tmp_path):
+    """The epoch loop stops once test RMSE improves by less than 1e-8 over the
+    previous epoch (sgd_Kernel.cu:1308-1317): with a learning rate too small
+    to move it, epochs 0 and 1 run and the loop ends.  The output and dump
+    directories are created as named, shell metacharacters included."""
+    c = goldens.Case("uniform_3k")
+    data = tmp_path / "data"
+    data.mkdir()
+    with open(data / "ds.train", "w") as f:
+        for (x, y, z), v in zip(c.input_xyz.tolist(), c.input_val.tolist()):
+            f.write("%d %d %d %.12g\n" % (x, y, z, v))
+    with open(data / "ds.test", "w") as f:
+        for (x, y, z), v in list(zip(c.input_xyz.tolist(), c.input_val.tolist()))[:200]:
+            f.write("%d %d %d %.12g\n" % (x, y, z, v))
+    marker = tmp_path / "ran"
+    out = tmp_path / ('o "q" $(touch %s)' % marker)
+    dump = tmp_path / "d;touch x"
+    I, J, K = c.dims
+    r = subprocess.run([bg.CLI_PATH, "ds", str(I), str(J), str(K), str(data), "0", str(out), "--epochs", "50",
+                        "--lr", "1e-12", "--seed", "5", "--dump-factors", str(dump)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert not marker.exists()
+    d = glob.glob(os.path.join(glob.escape(str(out)), "ds_*"))
+    assert len(d) == 1 and os.path.isdir(d[0])
+    lines = open(os.path.join(d[0], "error.txt")).read().splitlines()
+    assert [ln.split()[0] for ln in lines[1:]] == ["0", "1"]
+    assert "Epoch:1 test_RMSE=" in r.stdout and "Epoch:2 " not in r.stdout
+    assert (dump / "A.txt").is_file()

@@ -184,6 +184,45 @@ def test_binary_cache_round_trip_and_invalidation(tmp_path):
     assert np.array_equal(v4, v2)
 
 
+def test_binary_cache_with_out_of_range_payload_is_parsed_again(tmp_path):
+    """A cache whose header matches but whose coordinates break the shape
+    (a damaged file, a stamp collision) is not trusted: the text is parsed."""
+    p = tmp_path / "t.train"
+    p.write_text(_TRICKY)
+    cache = str(tmp_path / "t.train.btcbin")
+    want = bg.read_entries(str(p), 1, 10, 10, 10, cache=cache)
+    assert os.path.exists(cache)
+    with open(cache, "r+b") as f:
+        f.seek(48)  # first coordinate after the 48-byte header
+        f.write(np.array([10], np.int32).tobytes())  # x = I: out of range
+    st = os.stat(str(p))
+    got = bg.read_entries(str(p), 1, 10, 10, 10, cache=cache)
+    assert not bg.read_entries.from_cache
+    assert os.stat(str(p)).st_mtime_ns == st.st_mtime_ns
+    for a, b in zip(want, got):
+        assert np.array_equal(a, b)
+
+
+def test_context_rejects_out_of_range_coordinates_before_the_device():
+    """Train or test coordinates outside the shape fail with BTC_ERR_RANGE
+    before any device work, so no kernel can index past a factor."""
+    I, J, K = 6, 5, 4
+    tx = np.array([[0, 0, 0], [5, 4, 3], [1, 2, 3]], np.int32)
+    tv = np.ones(3)
+    cfg = bg.config(I=I, J=J, K=K, rank=4, block_s=2, resident_blocks=-1)
+    sched = bg.Schedule(cfg, tx)
+    for bad_test in (np.array([[0, 0, 4]], np.int32), np.array([[-1, 0, 0]], np.int32),
+                     np.array([[6, 0, 0]], np.int32)):
+        with pytest.raises(bg.BtcError) as e:
+            bg.Context(cfg, sched, tx, tv, bad_test, np.ones(1))
+        assert e.value.status == 8
+    # a train array other than the one the schedule was built from, with a
+    # coordinate out of range
+    with pytest.raises(bg.BtcError) as e:
+        bg.Context(cfg, sched, np.array([[0, 0, 0], [5, 5, 3], [1, 2, 3]], np.int32), tv, tx, tv)
+    assert e.value.status == 8
+
+
 def test_reader_rejects_out_of_range(tmp_path):
     p = tmp_path / "t.train"
     p.write_text("1 1 1 1.0\n0 1 1 2.0\n")

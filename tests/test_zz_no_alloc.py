@@ -1,8 +1,7 @@
 """The allocation-free error sums agree with the context's own evaluation.
 
-Callers that cannot call cudaMalloc -- code running while a stream is being
-captured into a CUDA graph, hosts whose framework owns every device
-allocation, allocation-free real-time loops -- use btc_eval_sums_noalloc,
+Callers that cannot call cudaMalloc -- hosts whose framework owns every
+device allocation, allocation-free real-time loops -- use btc_eval_sums_noalloc,
 whose only scratch is a static device array inside the library.  The inputs
 and outputs here are device buffers the test allocates itself (with torch);
 the entry point allocates nothing.  Two calls in a row share that scratch
@@ -73,3 +72,35 @@ def test_noalloc_rejects_sizes_beyond_scratch():
     assert st == ERR_RANGE
     torch.cuda.synchronize(dev)
     assert sums.cpu().tolist() == [7.0, 7.0, 7.0]  # nothing was launched
+
+
+def test_noalloc_padded_rows_and_empty_input():
+    """Rows stored with a stride above the rank (padding columns that must not
+    enter the dot products), and n = 0, which writes three zeros."""
+    R, stride = 12, 16
+    ctx, sx, sv, F = _context(bg.F32, R)
+    want = ctx.eval(bg.TEST)
+    dev = torch.device("cuda", 0)
+    xyz = torch.from_numpy(np.ascontiguousarray(sx, np.int32)).to(dev)
+    val = torch.from_numpy(np.ascontiguousarray(sv, np.float64)).to(dev)
+    fac = []
+    for f in F:
+        p = np.full((f.shape[0], stride), 1e3, np.float32)  # padding that would spoil any dot it entered
+        p[:, :R] = f
+        fac.append(torch.from_numpy(p).to(dev))
+    sums = torch.full((3,), -1.0, dtype=torch.float64, device=dev)
+    fn = bg.lib().btc_eval_sums_noalloc
+    st = fn(xyz.data_ptr(), val.data_ptr(), len(sv), fac[0].data_ptr(), fac[1].data_ptr(), fac[2].data_ptr(),
+            bg.F32, R, stride, sums.data_ptr(), None)
+    assert st == 0
+    torch.cuda.synchronize(dev)
+    got = sums.cpu().numpy()
+    assert got[0] == pytest.approx(want.sse, rel=1e-6)
+    assert got[1] == pytest.approx(want.sae, rel=1e-6)
+    sums.fill_(-1.0)
+    st = fn(xyz.data_ptr(), val.data_ptr(), 0, fac[0].data_ptr(), fac[1].data_ptr(), fac[2].data_ptr(),
+            bg.F32, R, stride, sums.data_ptr(), None)
+    assert st == 0
+    torch.cuda.synchronize(dev)
+    assert sums.cpu().tolist() == [0.0, 0.0, 0.0]
+    ctx.close()
