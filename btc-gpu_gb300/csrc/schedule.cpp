@@ -21,6 +21,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <set>
 #include <sstream>
 #include <thread>
@@ -297,6 +298,470 @@ btc_status blocking(const int32_t* xyz, int64_t n, int I, int J, int K, int bs, 
                 NB.ent.reserve(bs);
         }
       }
+    }
+    for (auto& b : blocks)
+        finish_block_codes(b);
+    for (int a = 0; a < 3; a++)
+        s.global_levels[a] = g[a];
+    return BTC_OK;
+}
+
+// The same blocking on host threads, bit-identical to blocking() above.
+//
+// Insertions interact in two ways only: through the leaf an entry lands in
+// (a subtree's evolution depends only on the entries routed into it, in
+// order, since internal nodes never change), and through the global levels
+// (every bucket code, and the split bit, is taken at them).  So entries are
+// processed in chunks: each chunk is routed against a snapshot of the tree,
+// grouped by snapshot leaf, and every group replays its entries into its own
+// subtree on a thread with the global levels held fixed.  A group stops at
+// the first entry whose split would raise a global level (an "event"): the
+// chunk is then replayed up to the earliest event, that entry is inserted
+// alone (raising the level), and the next chunk starts after it.  New blocks
+// receive their ids in the order the serial loop would allocate them: by
+// entry, then by split within the entry's re-split loop.
+namespace par {
+
+struct LBlock {
+    int32_t level[3];
+    uint64_t code[3];
+    std::vector<int32_t> ent;
+};
+
+struct Group {
+    int32_t leaf = 0, b0 = 0;      // snapshot leaf (global node) and its block
+    int32_t first = 0, count = 0;  // the group's entries in the chunk's grouped order
+    int64_t event = -1;            // chunk index of the entry that would raise a global level
+    bool bad = false;              // a bucket code out of range
+    bool split = false;            // the leaf split inside the chunk
+    int32_t napp = 0;              // entries appended to b0 (no split): app[first, first + napp)
+    std::vector<Node> nodes;       // when split: local subtree, [0] = the leaf
+    std::vector<LBlock> lb;        // when split: [0] = b0, then new blocks in creation order
+    std::vector<uint64_t> log;     // (entry << 8 | split seq) of each new block lb[1..]
+};
+
+inline int choose_axis(const int32_t* lv)
+{
+    if (lv[0] == lv[1] && lv[1] == lv[2])
+        return 0;
+    if (lv[1] < lv[0])
+        return 1;
+    if (lv[2] < lv[1])
+        return 2;
+    return -1;
+}
+
+// Replays the group's entries (chunk indices ascending, below `limit`) into
+// the subtree of its snapshot leaf with global levels g fixed.
+void run_group(Group& G, const int32_t* pts, const int64_t* codes, int64_t base, int64_t limit, const int* g,
+               int bs, const int32_t* xyz, const Axis* ax, const std::vector<Node>& gnodes,
+               const std::vector<BlockRec>& blocks, int32_t* app)
+{
+    G.event = -1;
+    G.bad = false;
+    G.split = false;
+    G.napp = 0;
+    G.nodes.clear();
+    G.lb.clear();
+    G.log.clear();
+    const std::vector<int32_t>& e0 = blocks[(size_t)G.b0].ent;
+    std::vector<int32_t> t1, t2;
+    for (int32_t q = 0; q < G.count; q++) {
+        const int64_t k = pts[G.first + q];
+        if (k >= limit)
+            return;
+        const int64_t i = base + k;
+        const int64_t* pc = codes + 3 * k;
+        int node = 0, id = 0;
+        if (!G.split) {
+            if ((int64_t)e0.size() + G.napp < bs) {
+                app[G.first + G.napp++] = (int32_t)i;
+                continue;
+            }
+            // the leaf's block is full: from here on the subtree is local
+            G.split = true;
+            G.nodes.push_back(gnodes[(size_t)G.leaf]);
+            G.nodes[0].block = 0;
+            LBlock b;
+            const BlockRec& B0 = blocks[(size_t)G.b0];
+            for (int a = 0; a < 3; a++) {
+                b.level[a] = B0.level[a];
+                b.code[a] = B0.code[a];
+            }
+            b.ent.reserve((size_t)bs + 1);
+            b.ent.assign(e0.begin(), e0.end());
+            b.ent.insert(b.ent.end(), app + G.first, app + G.first + G.napp);
+            G.lb.push_back(std::move(b));
+        } else {
+            node = route(G.nodes, 0, pc, g);
+            id = G.nodes[(size_t)node].block;
+            if ((int)G.lb[(size_t)id].ent.size() < bs) {
+                G.lb[(size_t)id].ent.push_back((int32_t)i);
+                continue;
+            }
+        }
+        const int32_t* p = xyz + 3 * i;
+        int seq = 0;
+        for (bool done = false; !done;) {
+            const int a = choose_axis(G.lb[(size_t)id].level);
+            if (a < 0 || G.lb[(size_t)id].level[a] + 1 > g[a]) {
+                G.event = k;  // the serial pass takes this entry
+                return;
+            }
+            G.lb[(size_t)id].level[a]++;
+            const int nb = (int)G.lb.size();
+            {
+                const int l = (int)G.nodes.size();
+                G.nodes.resize(G.nodes.size() + 2);
+                Node& P = G.nodes[(size_t)node];
+                const int ta = axis_of_h(P.h);
+                Node L = P, R = P;
+                L.h = R.h = P.h + 1;
+                L.left = L.right = R.left = R.right = -1;
+                L.len[ta] = R.len[ta] = P.len[ta] + 1;
+                L.code[ta] = P.code[ta] << 1;
+                R.code[ta] = (P.code[ta] << 1) | 1ULL;
+                L.block = id;
+                R.block = nb;
+                P.block = -1;
+                P.left = l;
+                P.right = l + 1;
+                G.nodes[(size_t)l] = L;
+                G.nodes[(size_t)l + 1] = R;
+            }
+            G.lb.emplace_back();
+            G.log.push_back(((uint64_t)k << 8) | (uint64_t)seq++);
+            LBlock& NB = G.lb[(size_t)nb];
+            LBlock& B = G.lb[(size_t)id];
+            for (int q2 = 0; q2 < 3; q2++) {
+                NB.level[q2] = B.level[q2];
+                NB.code[q2] = B.code[q2];
+            }
+            NB.code[a] = (B.code[a] << 1) | 1ULL;
+            B.code[a] = B.code[a] << 1;
+            t1.clear();
+            t2.clear();
+            for (int32_t e : B.ent) {
+                int64_t hv;
+                if (!ax[a].hx(g[a], xyz[3 * (int64_t)e + a], hv)) {
+                    G.bad = true;
+                    return;
+                }
+                ((hv & 1) == 0 ? t1 : t2).push_back(e);
+            }
+            int64_t hp;
+            if (!ax[a].hx(g[a], p[a], hp)) {
+                G.bad = true;
+                return;
+            }
+            const int bit = (int)(hp & 1);
+            if ((int)t1.size() < bs && (int)t2.size() < bs) {
+                done = true;
+                (bit == 0 ? t1 : t2).push_back((int32_t)i);
+                B.ent.assign(t1.begin(), t1.end());
+                NB.ent.assign(t2.begin(), t2.end());
+            } else if (bit == 0) {
+                B.ent.assign(t1.begin(), t1.end());
+                NB.ent.assign(t2.begin(), t2.end());
+                node = G.nodes[(size_t)node].left;
+            } else {
+                // the old block keeps its entries (block.cu:244-253)
+                NB.ent.assign(t2.begin(), t2.end());
+                id = nb;
+                node = G.nodes[(size_t)node].right;
+            }
+        }
+    }
+}
+
+}  // namespace par
+
+btc_status blocking_parallel(const int32_t* xyz, int64_t n, int I, int J, int K, int bs, int threads,
+                             Schedule& s)
+{
+    using namespace par;
+    Axis ax[3];
+    ax[0].init(I);
+    ax[1].init(J);
+    ax[2].init(K);
+    int g[3] = {1, 1, 1};
+    std::vector<Node> nodes(1);
+    std::vector<BlockRec>& blocks = s.blocks;
+    blocks.clear();
+    blocks.reserve((size_t)std::max<int64_t>(16, n / std::max(1, bs) * 2));
+    blocks.emplace_back();
+    for (int a = 0; a < 3; a++) {
+        blocks[0].level[a] = 1;
+        blocks[0].code[a] = 0;
+    }
+    const int T = std::max(1, std::min(threads, 64));
+    const int64_t CH_MIN = 1 << 12, CH_MAX = 1 << 22;
+    const int64_t cap = std::min<int64_t>(n, CH_MAX);
+    std::vector<int64_t> codes((size_t)cap * 3);
+    std::vector<int32_t> leaf((size_t)cap), pts((size_t)cap), app((size_t)cap), gid((size_t)cap);
+    std::vector<int32_t> group_of_node;
+    std::vector<Group> groups;
+    std::vector<int32_t> order;  // groups by size, largest first
+    std::vector<int32_t> t1, t2;
+
+    // a pool that runs fn(t) for t in [0, T) and waits
+    auto parallel = [&](int nt, const std::function<void(int)>& fn) {
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nt; t++)
+            pool.emplace_back(fn, t);
+        fn(0);
+        for (auto& th : pool)
+            th.join();
+    };
+
+    // the serial insertion of one entry from the root (blocking() above)
+    auto insert_one = [&](int64_t i) -> btc_status {
+        const int32_t* p = xyz + 3 * i;
+        int64_t pc[3];
+        for (int a = 0; a < 3; a++)
+            if (!ax[a].hx(g[a], p[a], pc[a]))
+                return BTC_ERR_RANGE;
+        int node = route(nodes, 0, pc, g);
+        int id = nodes[(size_t)node].block;
+        if ((int)blocks[(size_t)id].ent.size() < bs) {
+            blocks[(size_t)id].ent.push_back((int32_t)i);
+            return BTC_OK;
+        }
+        for (bool done = false; !done;) {
+            const int a = choose_axis(blocks[(size_t)id].level);
+            if (a < 0)
+                return BTC_ERR_STATE;
+            blocks[(size_t)id].level[a]++;
+            if (blocks[(size_t)id].level[a] > g[a])
+                g[a] = blocks[(size_t)id].level[a];
+            if (g[a] > 63)
+                return BTC_ERR_RANGE;
+            const int nb = (int)blocks.size();
+            {
+                const int l = (int)nodes.size();
+                nodes.resize(nodes.size() + 2);
+                Node& P = nodes[(size_t)node];
+                const int ta = axis_of_h(P.h);
+                Node L = P, R = P;
+                L.h = R.h = P.h + 1;
+                L.left = L.right = R.left = R.right = -1;
+                L.len[ta] = R.len[ta] = P.len[ta] + 1;
+                L.code[ta] = P.code[ta] << 1;
+                R.code[ta] = (P.code[ta] << 1) | 1ULL;
+                L.block = id;
+                R.block = nb;
+                P.block = -1;
+                P.left = l;
+                P.right = l + 1;
+                nodes[(size_t)l] = L;
+                nodes[(size_t)l + 1] = R;
+            }
+            blocks.emplace_back();
+            BlockRec& NB = blocks[(size_t)nb];
+            BlockRec& B = blocks[(size_t)id];
+            for (int q = 0; q < 3; q++) {
+                NB.level[q] = B.level[q];
+                NB.code[q] = B.code[q];
+            }
+            NB.code[a] = (B.code[a] << 1) | 1ULL;
+            B.code[a] = B.code[a] << 1;
+            t1.clear();
+            t2.clear();
+            for (int32_t e : B.ent) {
+                int64_t hv;
+                if (!ax[a].hx(g[a], xyz[3 * (int64_t)e + a], hv))
+                    return BTC_ERR_RANGE;
+                ((hv & 1) == 0 ? t1 : t2).push_back(e);
+            }
+            int64_t hp;
+            if (!ax[a].hx(g[a], p[a], hp))
+                return BTC_ERR_RANGE;
+            const int bit = (int)(hp & 1);
+            if ((int)t1.size() < bs && (int)t2.size() < bs) {
+                done = true;
+                (bit == 0 ? t1 : t2).push_back((int32_t)i);
+                B.ent.assign(t1.begin(), t1.end());
+                NB.ent.assign(t2.begin(), t2.end());
+            } else if (bit == 0) {
+                B.ent.assign(t1.begin(), t1.end());
+                NB.ent.assign(t2.begin(), t2.end());
+                node = nodes[(size_t)node].left;
+            } else {
+                NB.ent.assign(t2.begin(), t2.end());
+                id = nb;
+                node = nodes[(size_t)node].right;
+            }
+        }
+        return BTC_OK;
+    };
+
+    int64_t ch = CH_MIN;
+    for (int64_t base = 0; base < n;) {
+        const int64_t cn = std::min(ch, n - base);
+        // 1. bucket codes at the current global levels and snapshot leaves
+        std::atomic<int> bad(0);
+        {
+            const int nt = std::max(1, std::min<int>(T, (int)(cn / 4096) + 1));
+            parallel(nt, [&](int t) {
+                const int64_t lo = cn * t / nt, hi = cn * (t + 1) / nt;
+                for (int64_t k = lo; k < hi; k++) {
+                    const int32_t* p = xyz + 3 * (base + k);
+                    int64_t* pc = &codes[(size_t)(3 * k)];
+                    for (int a = 0; a < 3; a++)
+                        if (!ax[a].hx(g[a], p[a], pc[a])) {
+                            bad = 1;
+                            return;
+                        }
+                    leaf[(size_t)k] = route(nodes, 0, pc, g);
+                }
+            });
+        }
+        if (bad)
+            return BTC_ERR_RANGE;
+        // 2. groups by snapshot leaf, in order of first appearance; each
+        //    group's entries in chunk order
+        if (group_of_node.size() < nodes.size())
+            group_of_node.resize(nodes.size(), -1);
+        int32_t ng = 0;
+        for (int64_t k = 0; k < cn; k++) {
+            int32_t& q = group_of_node[(size_t)leaf[(size_t)k]];
+            if (q < 0) {
+                q = ng++;
+                if ((int32_t)groups.size() < ng)
+                    groups.emplace_back();
+                Group& G = groups[(size_t)q];
+                G.leaf = leaf[(size_t)k];
+                G.b0 = nodes[(size_t)G.leaf].block;
+                G.count = 0;
+            }
+            gid[(size_t)k] = q;
+            groups[(size_t)q].count++;
+        }
+        {
+            int32_t o = 0;
+            for (int32_t q = 0; q < ng; q++) {
+                groups[(size_t)q].first = o;
+                o += groups[(size_t)q].count;
+                groups[(size_t)q].count = 0;
+            }
+            for (int64_t k = 0; k < cn; k++) {
+                Group& G = groups[(size_t)gid[(size_t)k]];
+                pts[(size_t)(G.first + G.count++)] = (int32_t)k;
+            }
+            for (int32_t q = 0; q < ng; q++)
+                group_of_node[(size_t)groups[(size_t)q].leaf] = -1;
+        }
+        order.resize((size_t)ng);
+        for (int32_t q = 0; q < ng; q++)
+            order[(size_t)q] = q;
+        std::sort(order.begin(), order.end(),
+                  [&](int32_t a, int32_t b) { return groups[(size_t)a].count > groups[(size_t)b].count; });
+        // 3. replay every group on the threads (twice when an event cuts the
+        //    chunk short: the second pass stops before the earliest event)
+        int64_t limit = cn, event = -1;
+        for (int pass = 0; pass < 2; pass++) {
+            std::atomic<int32_t> next(0);
+            const int nt = std::max(1, std::min<int>(T, ng));
+            parallel(nt, [&](int) {
+                for (;;) {
+                    const int32_t q = next.fetch_add(1);
+                    if (q >= ng)
+                        return;
+                    run_group(groups[(size_t)order[(size_t)q]], pts.data(), codes.data(), base, limit, g, bs,
+                              xyz, ax, nodes, blocks, app.data());
+                }
+            });
+            event = -1;
+            for (int32_t q = 0; q < ng; q++) {
+                if (groups[(size_t)q].bad)
+                    return BTC_ERR_RANGE;
+                const int64_t e = groups[(size_t)q].event;
+                if (e >= 0 && (event < 0 || e < event))
+                    event = e;
+            }
+            if (event < 0)
+                break;
+            limit = event;  // replay up to the earliest event
+        }
+        if (event >= 0)
+            return BTC_ERR_STATE;  // the second pass cannot meet an event
+        // 4. commit: new block ids in serial allocation order, subtrees
+        //    spliced under their leaves
+        struct NewB {
+            uint64_t key;
+            int32_t group, local;
+        };
+        std::vector<NewB> nbs;
+        std::vector<int32_t> node_off((size_t)ng + 1, 0);
+        for (int32_t q = 0; q < ng; q++) {
+            const Group& G = groups[(size_t)q];
+            node_off[(size_t)q + 1] = node_off[(size_t)q] + (G.split ? (int32_t)G.nodes.size() - 1 : 0);
+            if (G.split)
+                for (size_t j = 0; j < G.log.size(); j++)
+                    nbs.push_back(NewB{G.log[j], q, (int32_t)j + 1});
+        }
+        std::sort(nbs.begin(), nbs.end(), [](const NewB& a, const NewB& b) { return a.key < b.key; });
+        const int32_t nb0 = (int32_t)blocks.size();
+        std::vector<std::vector<int32_t>> lmap((size_t)ng);
+        for (int32_t q = 0; q < ng; q++)
+            if (groups[(size_t)q].split) {
+                lmap[(size_t)q].assign(groups[(size_t)q].lb.size(), -1);
+                lmap[(size_t)q][0] = groups[(size_t)q].b0;
+            }
+        for (size_t r = 0; r < nbs.size(); r++)
+            lmap[(size_t)nbs[r].group][(size_t)nbs[r].local] = nb0 + (int32_t)r;
+        blocks.resize(blocks.size() + nbs.size());
+        const int32_t nn0 = (int32_t)nodes.size();
+        nodes.resize(nodes.size() + (size_t)node_off[(size_t)ng]);
+        {
+            std::atomic<int32_t> next(0);
+            const int nt = std::max(1, std::min<int>(T, ng / 64 + 1));
+            parallel(nt, [&](int) {
+                for (;;) {
+                    const int32_t q = next.fetch_add(1);
+                    if (q >= ng)
+                        return;
+                    Group& G = groups[(size_t)q];
+                    if (!G.split) {
+                        std::vector<int32_t>& e = blocks[(size_t)G.b0].ent;
+                        e.insert(e.end(), app.data() + G.first, app.data() + G.first + G.napp);
+                        continue;
+                    }
+                    const std::vector<int32_t>& m = lmap[(size_t)q];
+                    for (size_t j = 0; j < G.lb.size(); j++) {
+                        BlockRec& B = blocks[(size_t)m[j]];
+                        for (int a = 0; a < 3; a++) {
+                            B.level[a] = G.lb[j].level[a];
+                            B.code[a] = G.lb[j].code[a];
+                        }
+                        B.ent.swap(G.lb[j].ent);
+                        G.lb[j].ent.clear();
+                    }
+                    auto gnode = [&](int32_t l) { return l == 0 ? G.leaf : nn0 + node_off[(size_t)q] + l - 1; };
+                    for (size_t j = 0; j < G.nodes.size(); j++) {
+                        Node v = G.nodes[j];
+                        if (v.left >= 0) {
+                            v.left = gnode(v.left);
+                            v.right = gnode(v.right);
+                        }
+                        if (v.block >= 0)
+                            v.block = m[(size_t)v.block];
+                        nodes[(size_t)gnode((int32_t)j)] = v;
+                    }
+                }
+            });
+        }
+        if (limit < cn) {
+            // the event entry, alone: it raises a global level
+            btc_status rc = insert_one(base + limit);
+            if (rc != BTC_OK)
+                return rc;
+            base += limit + 1;
+            ch = std::max(CH_MIN, ch / 2);
+        } else {
+            base += cn;
+            ch = std::min(CH_MAX, ch * 2);
+        }
     }
     for (auto& b : blocks)
         finish_block_codes(b);
@@ -622,7 +1087,10 @@ btc_status build_schedule(const btc_config& cfg, const int32_t* xyz, int64_t n, 
     s.pss = cfg.parallel_sequence_size;
     s.train_nnz = n;
     double t0 = now_s();
-    btc_status rc = blocking(xyz, n, cfg.I, cfg.J, cfg.K, cfg.block_s, threads, s);
+    // one thread: the serial pass; several: the chunked pass (same result)
+    btc_status rc = threads > 1 && n >= (1 << 16)
+                        ? blocking_parallel(xyz, n, cfg.I, cfg.J, cfg.K, cfg.block_s, threads, s)
+                        : blocking(xyz, n, cfg.I, cfg.J, cfg.K, cfg.block_s, threads, s);
     if (rc != BTC_OK)
         return rc;
     double t1 = now_s();

@@ -104,6 +104,36 @@ def test_threaded_builder_equals_serial_builder():
         assert np.array_equal(x, y)
 
 
+@pytest.mark.parametrize("dims,nnz,zipf,block_s", [((20000, 20000, 5000), 300_000, (1.2, 1.2, 1.2), 16),
+                                                   ((50000, 500, 200000), 400_000, (1.5, 0.0, 1.5), 256),
+                                                   ((1000, 1000, 1000), 300_000, (1.3, 1.3, 1.3), 32),
+                                                   ((300, 200, 100), 200_000, (1.1, 1.1, 1.1), 8)])
+def test_chunked_blocking_equals_serial_blocking(dims, nnz, zipf, block_s):
+    """With several host threads the blocking runs in chunks: entries grouped
+    by the leaf they reach in a snapshot of the tree, each group replayed into
+    its own subtree on a thread, a chunk cut short where a split would raise a
+    global level.  Blocks (ids, levels, codes, entry order), strata and slots
+    must equal the one-thread insertion loop's.  Small block_s gives tens of
+    thousands of splits and many global-level changes."""
+    I, J, K = dims
+    tx, _, _, _ = bg.gen_tensor(I, J, K, nnz, zipf=zipf, gt_rank=2, train_frac=1.0, seed=nnz + block_s)
+    tx, _ = bg.shuffle(tx, np.zeros(len(tx)))
+    out = []
+    for threads in (1, 6):
+        s = bg.Schedule(bg.config(I=I, J=J, K=K, block_s=block_s, parallel_sequence_size=8, host_threads=threads,
+                                  resident_blocks=-1), tx)
+        meta, codes = s.blocks()
+        out.append((s, meta, codes))
+    (a, ma, ca), (b, mb, cb) = out
+    assert np.array_equal(ma, mb) and np.array_equal(ca, cb)
+    assert a.summary.num_blocks > 1000
+    for i in range(len(ma)):
+        assert np.array_equal(a.block_entries(i), b.block_entries(i)), i
+    assert a.strata() == b.strata()
+    for x, y in zip(a.groups(), b.groups()):
+        assert np.array_equal(x, y)
+
+
 def test_report_byte_identical(built, tmp_path):
     c, xyz, val, s = built
     p = tmp_path / "block_parallel.txt"
