@@ -147,12 +147,36 @@ struct Zipf {
         }
         for (int i = 0; i < n; i++)
             cdf[i] /= acc;
+        build_guide();
+    }
+    // guide[j] = first index whose cdf reaches j / G (G = 2^14, a table
+    // small enough to stay in cache).  For u in [j / G, (j + 1) / G) --
+    // j = floor(u * G) is exact, G being a power of two -- lower_bound(cdf, u)
+    // lies in [guide[j], guide[j + 1]], so a binary search over that range
+    // gives exactly lower_bound(cdf, u) (the guide-table inversion of Chen
+    // and Asau, 1974).  Skewed distributions keep most searches in the head.
+    static constexpr int G = 1 << 14;
+    std::vector<int> guide;
+    void build_guide()
+    {
+        if (s <= 0)
+            return;
+        guide.resize((size_t)G + 1);
+        int k = 0;
+        for (int j = 0; j <= G; j++) {
+            const double t = (double)j / (double)G;
+            while (k < n && cdf[(size_t)k] < t)
+                k++;
+            guide[(size_t)j] = k;
+        }
     }
     int sample(double u) const
     {
         if (s <= 0)
             return std::min(n - 1, (int)(u * n));
-        int k = (int)(std::lower_bound(cdf.begin(), cdf.end(), u) - cdf.begin());
+        const size_t j = std::min((size_t)G - 1, (size_t)(u * (double)G));
+        const int lo = guide[j], hi = std::min(n, guide[j + 1] + 1);
+        const int k = (int)(std::lower_bound(cdf.begin() + lo, cdf.begin() + hi, u) - cdf.begin());
         return std::min(k, n - 1);
     }
 };
@@ -365,6 +389,43 @@ void write_cache(const char* cache, const CacheHdr& hdr, const int32_t* xyz, con
 
 }  // namespace
 
+namespace {
+
+// std::shuffle of the indices 0..n-1 with std::mt19937(seed), then the
+// entries gathered in that order on host threads (every output slot is
+// written once) and copied back.
+template <typename Idx>
+void shuffled_gather(int32_t* xyz, double* val, int64_t n, uint32_t seed)
+{
+    std::vector<Idx> perm((size_t)n);
+    for (int64_t i = 0; i < n; i++)
+        perm[(size_t)i] = (Idx)i;
+    std::mt19937 rng(seed);
+    std::shuffle(perm.begin(), perm.end(), rng);
+    std::vector<int32_t> nx((size_t)n * 3);
+    std::vector<double> nv((size_t)n);
+    const int T = n >= (1 << 20) ? (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency())) : 1;
+    auto gather = [&](int t) {
+        for (int64_t i = n * t / T; i < n * (t + 1) / T; i++) {
+            const int64_t s = (int64_t)perm[(size_t)i];
+            nx[(size_t)(3 * i)] = xyz[3 * s];
+            nx[(size_t)(3 * i + 1)] = xyz[3 * s + 1];
+            nx[(size_t)(3 * i + 2)] = xyz[3 * s + 2];
+            nv[(size_t)i] = val[s];
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < T; t++)
+        pool.emplace_back(gather, t);
+    gather(0);
+    for (auto& th : pool)
+        th.join();
+    std::memcpy(xyz, nx.data(), sizeof(int32_t) * 3 * (size_t)n);
+    std::memcpy(val, nv.data(), sizeof(double) * (size_t)n);
+}
+
+}  // namespace
+
 extern "C" {
 
 btc_status btc_read_entries_cached(const char* path, const char* cache, int32_t coord_base, int32_t I, int32_t J,
@@ -402,23 +463,12 @@ btc_status btc_shuffle_entries(int32_t* xyz, double* val, int64_t n, uint32_t se
     if (n <= 1)
         return BTC_OK;
     // permute indices with the same std::shuffle/mt19937 sequence the
-    // reference applies to its vector<T_node>
-    std::vector<int64_t> perm((size_t)n);
-    for (int64_t i = 0; i < n; i++)
-        perm[(size_t)i] = i;
-    std::mt19937 rng(seed);
-    std::shuffle(perm.begin(), perm.end(), rng);
-    std::vector<int32_t> nx((size_t)n * 3);
-    std::vector<double> nv((size_t)n);
-    for (int64_t i = 0; i < n; i++) {
-        int64_t s = perm[(size_t)i];
-        nx[3 * i] = xyz[3 * s];
-        nx[3 * i + 1] = xyz[3 * s + 1];
-        nx[3 * i + 2] = xyz[3 * s + 2];
-        nv[i] = val[s];
-    }
-    std::memcpy(xyz, nx.data(), sizeof(int32_t) * 3 * (size_t)n);
-    std::memcpy(val, nv.data(), sizeof(double) * (size_t)n);
+    // reference applies to its vector<T_node> (32-bit indices when they
+    // suffice: the same permutation, half the memory traffic of its swaps)
+    if (n <= INT32_MAX)
+        shuffled_gather<int32_t>(xyz, val, n, seed);
+    else
+        shuffled_gather<int64_t>(xyz, val, n, seed);
     return BTC_OK;
 }
 
@@ -438,63 +488,158 @@ btc_status btc_gen_tensor(const btc_gen_spec* sp, int32_t** txyz, double** tval,
     for (int a = 0; a < 3; a++)
         z[a].init(dims[a], sp->zipf_s[a]);
     const uint64_t JK = (uint64_t)sp->J * (uint64_t)sp->K;
-    // open-addressing set of cell keys; entries kept in first-draw order
-    uint64_t cap = 1;
-    while (cap < (uint64_t)sp->nnz * 2 + 16)
-        cap <<= 1;
-    std::vector<uint64_t> table(cap, ~0ULL);
+    // The entries are the first nnz distinct cells in draw order (draw d
+    // picks its three indices from hash(seed, d, axis)).  Draws are taken in
+    // batches on host threads; each cell key goes to one of 4096 partitions
+    // by its hash, and every partition, on its own thread, inserts its keys
+    // into its own open-addressing set in draw order, marking the draws that
+    // saw a cell first.  The marked draws, in order, are the entries: the
+    // result does not depend on the thread count.  Many partitions keep each
+    // set small enough to stay in cache while its keys are inserted.
+    constexpr int P = 4096;
+    struct PartSet {
+        std::vector<uint64_t> t;
+        uint64_t used = 0;
+        bool insert(uint64_t k)
+        {
+            if (2 * (used + 1) > t.size()) {
+                std::vector<uint64_t> old;
+                old.swap(t);
+                t.assign(std::max<size_t>(1024, old.size() * 2), ~0ULL);
+                for (uint64_t v : old)
+                    if (v != ~0ULL) {
+                        uint64_t h = mix64(v) & (t.size() - 1);
+                        while (t[h] != ~0ULL)
+                            h = (h + 1) & (t.size() - 1);
+                        t[h] = v;
+                    }
+            }
+            uint64_t h = mix64(k) & (t.size() - 1);
+            while (t[h] != ~0ULL) {
+                if (t[h] == k)
+                    return false;
+                h = (h + 1) & (t.size() - 1);
+            }
+            t[h] = k;
+            used++;
+            return true;
+        }
+    };
+    std::vector<PartSet> sets(P);
+    {
+        size_t per = 1024;
+        while (per < (size_t)(2.5 * (double)sp->nnz / P))
+            per <<= 1;
+        for (auto& ps : sets)
+            ps.t.assign(per, ~0ULL);
+    }
     std::vector<uint64_t> keys;
     keys.reserve((size_t)sp->nnz);
     uint64_t drawn = 0;
-    const uint64_t batch = 1 << 22;
+    const uint64_t batch = (uint64_t)std::min<int64_t>(1LL << 24, std::max<int64_t>(1LL << 16, sp->nnz));
     std::vector<uint64_t> cand(batch);
+    std::vector<uint16_t> part_of(batch);
+    std::vector<uint8_t> first(batch);
+    std::vector<uint32_t> by_part(batch);
+    const int T = std::max(1, std::min(threads, 64));
+    std::vector<uint32_t> cnt((size_t)T * P), pos((size_t)T * P);
+    std::vector<uint32_t> part_off(P + 1);
+    auto run = [&](int nt, const auto& fn) {
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nt; t++)
+            pool.emplace_back(fn, t);
+        fn(0);
+        for (auto& th : pool)
+            th.join();
+    };
     while ((int64_t)keys.size() < sp->nnz) {
-        std::atomic<uint64_t> next(0);
-        auto work = [&]() {
+        // draws of this batch: keys and partitions; per-thread partition counts
+        run(T, [&](int t) {
+            const uint64_t lo = batch * (uint64_t)t / (uint64_t)T, hi = batch * (uint64_t)(t + 1) / (uint64_t)T;
+            uint32_t* c = &cnt[(size_t)t * P];
+            std::fill(c, c + P, 0u);
+            for (uint64_t i = lo; i < hi; i++) {
+                const uint64_t d = drawn + i;
+                const uint64_t x = (uint64_t)z[0].sample(unit(hash4(sp->seed, 11, d, 0)));
+                const uint64_t y = (uint64_t)z[1].sample(unit(hash4(sp->seed, 11, d, 1)));
+                const uint64_t w = (uint64_t)z[2].sample(unit(hash4(sp->seed, 11, d, 2)));
+                const uint64_t k = x * JK + y * (uint64_t)sp->K + w;
+                cand[i] = k;
+                const uint16_t q = (uint16_t)(mix64(k ^ 0x5851F42D4C957F2DULL) >> 52);
+                part_of[i] = q;
+                c[q]++;
+            }
+        });
+        // draws grouped by partition, each partition's in draw order
+        uint32_t o = 0;
+        for (int q = 0; q < P; q++) {
+            part_off[(size_t)q] = o;
+            for (int t = 0; t < T; t++) {
+                pos[(size_t)t * P + q] = o;
+                o += cnt[(size_t)t * P + q];
+            }
+        }
+        part_off[P] = o;
+        run(T, [&](int t) {
+            const uint64_t lo = batch * (uint64_t)t / (uint64_t)T, hi = batch * (uint64_t)(t + 1) / (uint64_t)T;
+            uint32_t* ps = &pos[(size_t)t * P];
+            for (uint64_t i = lo; i < hi; i++)
+                by_part[ps[part_of[i]]++] = (uint32_t)i;
+        });
+        std::atomic<int> nextp(0);
+        run(T, [&](int) {
             for (;;) {
-                uint64_t b0 = next.fetch_add(65536);
-                if (b0 >= batch)
-                    break;
-                uint64_t b1 = std::min(batch, b0 + 65536);
-                for (uint64_t i = b0; i < b1; i++) {
-                    uint64_t d = drawn + i;
-                    uint64_t x = (uint64_t)z[0].sample(unit(hash4(sp->seed, 11, d, 0)));
-                    uint64_t y = (uint64_t)z[1].sample(unit(hash4(sp->seed, 11, d, 1)));
-                    uint64_t w = (uint64_t)z[2].sample(unit(hash4(sp->seed, 11, d, 2)));
-                    cand[i] = x * JK + y * (uint64_t)sp->K + w;
+                const int q = nextp.fetch_add(1);
+                if (q >= P)
+                    return;
+                PartSet& S = sets[(size_t)q];
+                for (uint32_t j = part_off[(size_t)q]; j < part_off[(size_t)q + 1]; j++) {
+                    const uint32_t i = by_part[j];
+                    first[i] = S.insert(cand[i]) ? 1 : 0;
                 }
             }
-        };
-        std::vector<std::thread> pool;
-        for (int t = 1; t < threads; t++)
-            pool.emplace_back(work);
-        work();
-        for (auto& t : pool)
-            t.join();
-        for (uint64_t i = 0; i < batch && (int64_t)keys.size() < sp->nnz; i++) {
-            uint64_t k = cand[i];
-            uint64_t h = mix64(k) & (cap - 1);
-            while (table[h] != ~0ULL && table[h] != k)
-                h = (h + 1) & (cap - 1);
-            if (table[h] == ~0ULL) {
-                table[h] = k;
-                keys.push_back(k);
-            }
+        });
+        // the batch's new cells, in draw order, up to nnz in all
+        {
+            std::vector<int64_t> nf((size_t)T + 1, 0);
+            run(T, [&](int t) {
+                const uint64_t lo = batch * (uint64_t)t / (uint64_t)T, hi = batch * (uint64_t)(t + 1) / (uint64_t)T;
+                int64_t c = 0;
+                for (uint64_t i = lo; i < hi; i++)
+                    c += first[i];
+                nf[(size_t)t + 1] = c;
+            });
+            for (int t = 0; t < T; t++)
+                nf[(size_t)t + 1] += nf[(size_t)t];
+            const size_t k0 = keys.size();
+            const int64_t room = sp->nnz - (int64_t)k0;
+            keys.resize(k0 + (size_t)std::min<int64_t>(room, nf[(size_t)T]));
+            run(T, [&](int t) {
+                const uint64_t lo = batch * (uint64_t)t / (uint64_t)T, hi = batch * (uint64_t)(t + 1) / (uint64_t)T;
+                int64_t o = nf[(size_t)t];
+                for (uint64_t i = lo; i < hi && o < room; i++)
+                    if (first[i])
+                        keys[k0 + (size_t)o++] = cand[i];
+            });
         }
         drawn += batch;
         if (drawn > (uint64_t)sp->nnz * 1000 + (1ULL << 26))
             return BTC_ERR_RANGE;  // distribution too concentrated for the requested count
     }
-    std::vector<uint64_t>().swap(table);
+    std::vector<PartSet>().swap(sets);
     const int64_t n = (int64_t)keys.size();
     const int R = sp->gt_rank;
     // ground-truth factors
     std::vector<double> gt[3];
     for (int a = 0; a < 3 && R > 0; a++) {
-        gt[a].resize((size_t)dims[a] * R);
-        for (int64_t i = 0; i < (int64_t)dims[a] * R; i++)
-            gt[a][(size_t)i] = sp->gt_std * normal(hash4(sp->seed, 21 + a, (uint64_t)i, 0),
-                                                   hash4(sp->seed, 21 + a, (uint64_t)i, 1));
+        const int64_t m = (int64_t)dims[a] * R;
+        gt[a].resize((size_t)m);
+        run(m >= (1 << 20) ? T : 1, [&](int t) {
+            const int nt = m >= (1 << 20) ? T : 1;
+            for (int64_t i = m * t / nt; i < m * (t + 1) / nt; i++)
+                gt[a][(size_t)i] = sp->gt_std * normal(hash4(sp->seed, 21 + a, (uint64_t)i, 0),
+                                                       hash4(sp->seed, 21 + a, (uint64_t)i, 1));
+        });
     }
     std::vector<int32_t> xyz((size_t)n * 3);
     std::vector<double> val((size_t)n);
@@ -542,25 +687,42 @@ btc_status btc_gen_tensor(const btc_gen_spec* sp, int32_t** txyz, double** tval,
         for (double& v : val)
             v /= mx;
     }
-    int64_t a = 0, b = 0;
-    for (int64_t i = 0; i < n; i++)
-        (is_train[(size_t)i] ? a : b)++;
+    // train and test entries keep their order; ranges of entries are split
+    // on threads, each writing at the offsets the ranges before it leave
+    const int TS = n >= (1 << 20) ? T : 1;
+    std::vector<int64_t> na((size_t)TS + 1, 0), nbv((size_t)TS + 1, 0);
+    run(TS, [&](int t) {
+        const int64_t lo = n * t / TS, hi = n * (t + 1) / TS;
+        int64_t c = 0;
+        for (int64_t i = lo; i < hi; i++)
+            c += is_train[(size_t)i];
+        na[(size_t)t + 1] = c;
+        nbv[(size_t)t + 1] = (hi - lo) - c;
+    });
+    for (int t = 0; t < TS; t++) {
+        na[(size_t)t + 1] += na[(size_t)t];
+        nbv[(size_t)t + 1] += nbv[(size_t)t];
+    }
+    const int64_t a = na[(size_t)TS], b = nbv[(size_t)TS];
     *txyz = (int32_t*)std::malloc(sizeof(int32_t) * 3 * (size_t)std::max<int64_t>(a, 1));
     *tval = (double*)std::malloc(sizeof(double) * (size_t)std::max<int64_t>(a, 1));
     *sxyz = (int32_t*)std::malloc(sizeof(int32_t) * 3 * (size_t)std::max<int64_t>(b, 1));
     *sval = (double*)std::malloc(sizeof(double) * (size_t)std::max<int64_t>(b, 1));
     if (!*txyz || !*tval || !*sxyz || !*sval)
         return BTC_ERR_ALLOC;
-    int64_t ia = 0, ib = 0;
-    for (int64_t i = 0; i < n; i++) {
-        if (is_train[(size_t)i]) {
-            std::memcpy(*txyz + 3 * ia, &xyz[3 * i], 12);
-            (*tval)[ia++] = val[(size_t)i];
-        } else {
-            std::memcpy(*sxyz + 3 * ib, &xyz[3 * i], 12);
-            (*sval)[ib++] = val[(size_t)i];
+    run(TS, [&](int t) {
+        const int64_t lo = n * t / TS, hi = n * (t + 1) / TS;
+        int64_t ia = na[(size_t)t], ib = nbv[(size_t)t];
+        for (int64_t i = lo; i < hi; i++) {
+            if (is_train[(size_t)i]) {
+                std::memcpy(*txyz + 3 * ia, &xyz[3 * i], 12);
+                (*tval)[ia++] = val[(size_t)i];
+            } else {
+                std::memcpy(*sxyz + 3 * ib, &xyz[3 * i], 12);
+                (*sval)[ib++] = val[(size_t)i];
+            }
         }
-    }
+    });
     *ntr = a;
     *nte = b;
     return BTC_OK;
