@@ -122,6 +122,40 @@ inline int route(const std::vector<Node>& nodes, int node, const int64_t* pc, co
     }
 }
 
+// The tree for routing only, 16 bytes a node: a split node's children sit
+// at left and left + 1 (both passes allocate them as a pair); a leaf has
+// left = -1.  want / len: the left child's code and length on the split
+// axis.
+struct RNode {
+    int32_t left = -1;
+    uint8_t axis = 0, len = 0;
+    uint16_t pad = 0;
+    uint64_t want = 0;
+};
+
+inline RNode rnode_of(const Node& P)
+{
+    RNode r;
+    if (P.left >= 0) {
+        const int a = axis_of_h(P.h);
+        r.left = P.left;
+        r.axis = (uint8_t)a;
+        r.len = (uint8_t)(P.len[a] + 1);
+        r.want = P.code[a] << 1;
+    }
+    return r;
+}
+
+inline int route_fast(const RNode* rn, int node, const int64_t* pc, const int* g)
+{
+    for (;;) {
+        const RNode& P = rn[node];
+        if (P.left < 0)
+            return node;
+        node = prefix_bits(pc[P.axis], g[P.axis], P.len) == P.want ? P.left : P.left + 1;
+    }
+}
+
 btc_status blocking(const int32_t* xyz, int64_t n, int I, int J, int K, int bs, int threads, Schedule& s)
 {
     Axis ax[3];
@@ -486,6 +520,7 @@ btc_status blocking_parallel(const int32_t* xyz, int64_t n, int I, int J, int K,
     ax[2].init(K);
     int g[3] = {1, 1, 1};
     std::vector<Node> nodes(1);
+    std::vector<RNode> rnodes(1);
     std::vector<BlockRec>& blocks = s.blocks;
     blocks.clear();
     blocks.reserve((size_t)std::max<int64_t>(16, n / std::max(1, bs) * 2));
@@ -498,8 +533,9 @@ btc_status blocking_parallel(const int32_t* xyz, int64_t n, int I, int J, int K,
     const int64_t CH_MIN = 1 << 12, CH_MAX = 1 << 22;
     const int64_t cap = std::min<int64_t>(n, CH_MAX);
     std::vector<int64_t> codes((size_t)cap * 3);
-    std::vector<int32_t> leaf((size_t)cap), pts((size_t)cap), app((size_t)cap), gid((size_t)cap);
+    std::vector<int32_t> leaf((size_t)cap), pts((size_t)cap), app((size_t)cap);
     std::vector<int32_t> group_of_node;
+    std::vector<std::vector<int32_t>> tcount, tfirst;  // per grouping thread: count per leaf, leaves first seen
     std::vector<Group> groups;
     std::vector<int32_t> order;  // groups by size, largest first
     std::vector<int32_t> t1, t2;
@@ -521,7 +557,7 @@ btc_status blocking_parallel(const int32_t* xyz, int64_t n, int I, int J, int K,
         for (int a = 0; a < 3; a++)
             if (!ax[a].hx(g[a], p[a], pc[a]))
                 return BTC_ERR_RANGE;
-        int node = route(nodes, 0, pc, g);
+        int node = route_fast(rnodes.data(), 0, pc, g);
         int id = nodes[(size_t)node].block;
         if ((int)blocks[(size_t)id].ent.size() < bs) {
             blocks[(size_t)id].ent.push_back((int32_t)i);
@@ -555,6 +591,10 @@ btc_status blocking_parallel(const int32_t* xyz, int64_t n, int I, int J, int K,
                 P.right = l + 1;
                 nodes[(size_t)l] = L;
                 nodes[(size_t)l + 1] = R;
+                rnodes.resize(nodes.size());
+                rnodes[(size_t)node] = rnode_of(nodes[(size_t)node]);
+                rnodes[(size_t)l] = RNode();
+                rnodes[(size_t)l + 1] = RNode();
             }
             blocks.emplace_back();
             BlockRec& NB = blocks[(size_t)nb];
@@ -612,44 +652,73 @@ btc_status blocking_parallel(const int32_t* xyz, int64_t n, int I, int J, int K,
                             bad = 1;
                             return;
                         }
-                    leaf[(size_t)k] = route(nodes, 0, pc, g);
+                    leaf[(size_t)k] = route_fast(rnodes.data(), 0, pc, g);
                 }
             });
         }
         if (bad)
             return BTC_ERR_RANGE;
-        // 2. groups by snapshot leaf, in order of first appearance; each
-        //    group's entries in chunk order
+        // 2. groups by snapshot leaf (numbered in order of first appearance
+        //    in the chunk); each group's entries in chunk order.  Threads
+        //    count their share of the chunk per leaf, then write their
+        //    entries at the offsets the shares before them leave.
         if (group_of_node.size() < nodes.size())
             group_of_node.resize(nodes.size(), -1);
+        const int ntg = std::max(1, std::min<int>(T, (int)(cn / 65536) + 1));
+        if ((int)tcount.size() < ntg)
+            tcount.resize((size_t)ntg);
+        for (int t = 0; t < ntg; t++)
+            if (tcount[(size_t)t].size() < nodes.size())
+                tcount[(size_t)t].resize(nodes.size(), 0);
+        tfirst.assign((size_t)ntg, std::vector<int32_t>());
+        parallel(ntg, [&](int t) {
+            const int64_t lo = cn * t / ntg, hi = cn * (t + 1) / ntg;
+            std::vector<int32_t>& c = tcount[(size_t)t];
+            for (int64_t k = lo; k < hi; k++) {
+                const int32_t l = leaf[(size_t)k];
+                if (c[(size_t)l]++ == 0)
+                    tfirst[(size_t)t].push_back(l);
+            }
+        });
         int32_t ng = 0;
-        for (int64_t k = 0; k < cn; k++) {
-            int32_t& q = group_of_node[(size_t)leaf[(size_t)k]];
-            if (q < 0) {
+        for (int t = 0; t < ntg; t++)
+            for (int32_t l : tfirst[(size_t)t]) {
+                int32_t& q = group_of_node[(size_t)l];
+                if (q >= 0)
+                    continue;
                 q = ng++;
                 if ((int32_t)groups.size() < ng)
                     groups.emplace_back();
                 Group& G = groups[(size_t)q];
-                G.leaf = leaf[(size_t)k];
-                G.b0 = nodes[(size_t)G.leaf].block;
+                G.leaf = l;
+                G.b0 = nodes[(size_t)l].block;
                 G.count = 0;
             }
-            gid[(size_t)k] = q;
-            groups[(size_t)q].count++;
-        }
         {
+            // per group, each thread's write offset; tcount becomes that offset
             int32_t o = 0;
             for (int32_t q = 0; q < ng; q++) {
-                groups[(size_t)q].first = o;
-                o += groups[(size_t)q].count;
-                groups[(size_t)q].count = 0;
+                Group& G = groups[(size_t)q];
+                G.first = o;
+                for (int t = 0; t < ntg; t++) {
+                    int32_t& c = tcount[(size_t)t][(size_t)G.leaf];
+                    const int32_t k = c;
+                    c = o;
+                    o += k;
+                }
+                G.count = o - G.first;
             }
-            for (int64_t k = 0; k < cn; k++) {
-                Group& G = groups[(size_t)gid[(size_t)k]];
-                pts[(size_t)(G.first + G.count++)] = (int32_t)k;
-            }
-            for (int32_t q = 0; q < ng; q++)
+            parallel(ntg, [&](int t) {
+                const int64_t lo = cn * t / ntg, hi = cn * (t + 1) / ntg;
+                std::vector<int32_t>& c = tcount[(size_t)t];
+                for (int64_t k = lo; k < hi; k++)
+                    pts[(size_t)c[(size_t)leaf[(size_t)k]]++] = (int32_t)k;
+            });
+            for (int32_t q = 0; q < ng; q++) {
                 group_of_node[(size_t)groups[(size_t)q].leaf] = -1;
+                for (int t = 0; t < ntg; t++)
+                    tcount[(size_t)t][(size_t)groups[(size_t)q].leaf] = 0;
+            }
         }
         order.resize((size_t)ng);
         for (int32_t q = 0; q < ng; q++)
@@ -713,6 +782,7 @@ btc_status blocking_parallel(const int32_t* xyz, int64_t n, int I, int J, int K,
         blocks.resize(blocks.size() + nbs.size());
         const int32_t nn0 = (int32_t)nodes.size();
         nodes.resize(nodes.size() + (size_t)node_off[(size_t)ng]);
+        rnodes.resize(nodes.size());
         {
             std::atomic<int32_t> next(0);
             const int nt = std::max(1, std::min<int>(T, ng / 64 + 1));
@@ -747,6 +817,7 @@ btc_status blocking_parallel(const int32_t* xyz, int64_t n, int I, int J, int K,
                         if (v.block >= 0)
                             v.block = m[(size_t)v.block];
                         nodes[(size_t)gnode((int32_t)j)] = v;
+                        rnodes[(size_t)gnode((int32_t)j)] = rnode_of(v);
                     }
                 }
             });
@@ -771,14 +842,22 @@ btc_status blocking_parallel(const int32_t* xyz, int64_t n, int I, int J, int K,
 }
 
 // search_parallel_block_Tree as first-fit in ascending block id.
+//
+// A block joins the lowest-numbered stratum none of whose members it meets
+// on any axis (two blocks meet on an axis when their dyadic intervals
+// nest).  On skewed inputs almost every refusal comes from the head of an
+// axis: blocks that contain the same few hottest buckets all nest, so the
+// scan would re-test them stratum by stratum.  Per axis the 64 finest
+// buckets at the axis' global level ("hot buckets") are indexed by a binary
+// tree of 127 ranges; each range keeps a bitset of the strata holding a
+// member that covers one of its buckets.  A block covering hot buckets (an
+// aligned range, one tree node) certainly meets every stratum in its node's
+// bitset on that axis, so the scan skips those strata 64 at a time and runs
+// the exact test only on the rest.  Skipping only what the exact test would
+// refuse leaves the first fit unchanged.
 void strata_first_fit(Schedule& s, int threads)
 {
-    // A stratum's members are pairwise disjoint on every axis, so the measure
-    // of an axis they cover is the sum of their dyadic interval lengths
-    // (axis = 2^63 units, a level-L id covers 2^(64-L)).  A block needs at
-    // least its own length free on each axis, and a stratum that covers a
-    // whole axis can never take another block: both only skip strata the
-    // exact test would reject, so the first fit is unchanged.
+    (void)threads;
     const uint64_t FULL = 1ULL << 63;
     struct St {
         uint64_t bins[3] = {0, 0, 0};
@@ -786,8 +865,6 @@ void strata_first_fit(Schedule& s, int threads)
         std::vector<int32_t> mem;
     };
     std::vector<St> st;
-    std::vector<int32_t> open;  // strata that can still take a block, in creation order
-    size_t closed_since = 0;
     const auto& B = s.blocks;
     auto fits = [&](const St& S, const BlockRec& cb, const uint64_t* len) {
         if (FULL - S.used[0] < len[0] || FULL - S.used[1] < len[1] || FULL - S.used[2] < len[2])
@@ -801,79 +878,94 @@ void strata_first_fit(Schedule& s, int threads)
         }
         return true;
     };
-    // The scan over the open strata for one block is read-only, so long
-    // scans are split into contiguous shares of the open list, one per
-    // thread; a share stops at its first fit or once a lower share has found
-    // one, and the lowest position found is the first fit.
-    const int T = std::max(1, std::min(threads, 64));
-    const size_t PAR_MIN = 4096;
-    std::atomic<int> gen(0), done(0);
-    std::atomic<bool> quit(false);
-    std::atomic<int64_t> best(INT64_MAX);
-    const BlockRec* cur = nullptr;
-    uint64_t cur_len[3] = {0, 0, 0};
-    size_t n_open = 0;
-    auto scan = [&](int t) {
-        const size_t lo = n_open * (size_t)t / (size_t)T, hi = n_open * (size_t)(t + 1) / (size_t)T;
-        for (size_t q = lo; q < hi; q++) {
-            if ((int64_t)q >= best.load(std::memory_order_relaxed))
-                return;
-            if (fits(st[(size_t)open[q]], *cur, cur_len)) {
-                int64_t b0 = best.load(std::memory_order_relaxed);
-                while ((int64_t)q < b0 && !best.compare_exchange_weak(b0, (int64_t)q, std::memory_order_relaxed))
-                    ;
-                return;
-            }
+    // hot-bucket tree node of a block on axis a: 0 when it covers no hot
+    // bucket, else the heap index (1 = all hot buckets) of its aligned range
+    int hb[3], hlog[3];
+    for (int a = 0; a < 3; a++) {
+        const int g1 = s.global_levels[a] - 1;  // code bits at the global level
+        hlog[a] = std::min(6, g1);
+        hb[a] = 1 << hlog[a];
+    }
+    auto hot_node = [&](const BlockRec& b, int a) -> int {
+        const int g1 = s.global_levels[a] - 1, m = b.level[a] - 1;
+        // b covers the global-level buckets whose top m bits equal its code
+        const int sh = g1 - m;
+        if (sh >= 63)
+            return 1;
+        const uint64_t lo = b.code[a] << sh;
+        if (lo >= (uint64_t)hb[a])
+            return 0;
+        const int t = std::min(sh, hlog[a]);  // log2 of the covered hot range
+        return (int)((hb[a] + lo) >> t);
+    };
+    // bitsets over strata: per axis and tree node, and the closed strata
+    std::vector<std::vector<uint64_t>> tb(3 * 128);
+    std::vector<uint64_t> closed;
+    size_t words = 0;
+    auto grow = [&](size_t nst) {
+        const size_t need = (nst + 63) / 64;
+        if (need <= words)
+            return;
+        const size_t nw = std::max<size_t>(need, words * 2 + 16);
+        for (auto& v : tb)
+            if (!v.empty() || true)
+                v.resize(nw, 0);
+        closed.resize(nw, 0);
+        words = nw;
+    };
+    auto set_bit = [](std::vector<uint64_t>& v, size_t i) { v[i >> 6] |= 1ULL << (i & 63); };
+    // mark stratum k in every node whose range meets node u's: u, its
+    // ancestors and its descendants
+    auto mark = [&](int a, int u, size_t k) {
+        for (int v = u; v >= 1; v >>= 1)
+            set_bit(tb[(size_t)a * 128 + (size_t)v], k);
+        int lo = u, hi = u;
+        while ((lo << 1) < 2 * hb[a]) {
+            lo <<= 1;
+            hi = (hi << 1) | 1;
+            for (int v = lo; v <= hi; v++)
+                set_bit(tb[(size_t)a * 128 + (size_t)v], k);
         }
     };
-    std::vector<std::thread> pool;
-    for (int t = 1; t < T; t++)
-        pool.emplace_back([&, t] {
-            int seen = 0;
-            for (;;) {
-                int g;
-                while ((g = gen.load(std::memory_order_acquire)) == seen)
-                    std::this_thread::yield();
-                seen = g;
-                if (quit.load(std::memory_order_acquire))
-                    return;
-                scan(t);
-                done.fetch_add(1, std::memory_order_acq_rel);
-            }
-        });
     for (int32_t b = 0; b < (int32_t)B.size(); b++) {
         if (B[b].ent.empty())
             continue;
         const BlockRec& cb = B[b];
         uint64_t len[3];
-        for (int a = 0; a < 3; a++)
+        int node[3];
+        for (int a = 0; a < 3; a++) {
             len[a] = 1ULL << (64 - cb.level[a]);
+            node[a] = hot_node(cb, a);
+        }
+        const uint64_t* cx = node[0] ? tb[(size_t)node[0]].data() : nullptr;
+        const uint64_t* cy = node[1] ? tb[128 + (size_t)node[1]].data() : nullptr;
+        const uint64_t* cz = node[2] ? tb[256 + (size_t)node[2]].data() : nullptr;
         int32_t found = -1;
-        if (T > 1 && open.size() >= PAR_MIN) {
-            cur = &cb;
-            for (int a = 0; a < 3; a++)
-                cur_len[a] = len[a];
-            n_open = open.size();
-            best.store(INT64_MAX, std::memory_order_relaxed);
-            done.store(0, std::memory_order_relaxed);
-            gen.fetch_add(1, std::memory_order_acq_rel);
-            scan(0);
-            while (done.load(std::memory_order_acquire) < T - 1)
-                std::this_thread::yield();
-            const int64_t q = best.load(std::memory_order_relaxed);
-            if (q != INT64_MAX)
-                found = open[(size_t)q];
-        } else {
-            for (int32_t k : open)
-                if (fits(st[(size_t)k], cb, len)) {
-                    found = k;
+        const size_t nst = st.size();
+        for (size_t w = 0; w * 64 < nst && found < 0; w++) {
+            uint64_t busy = closed[w];
+            if (cx)
+                busy |= cx[w];
+            if (cy)
+                busy |= cy[w];
+            if (cz)
+                busy |= cz[w];
+            uint64_t cand = ~busy;
+            if ((w + 1) * 64 > nst)
+                cand &= (1ULL << (nst - w * 64)) - 1ULL;
+            while (cand) {
+                const size_t k = w * 64 + (size_t)__builtin_ctzll(cand);
+                cand &= cand - 1;
+                if (fits(st[k], cb, len)) {
+                    found = (int32_t)k;
                     break;
                 }
+            }
         }
         if (found < 0) {
             found = (int32_t)st.size();
             st.emplace_back();
-            open.push_back(found);
+            grow(st.size());
         }
         St& S = st[(size_t)found];
         S.mem.push_back(b);
@@ -882,21 +974,12 @@ void strata_first_fit(Schedule& s, int threads)
             S.bins[a] |= cb.bins[a];
             S.used[a] += len[a];
             full |= S.used[a] >= FULL;
+            if (node[a])
+                mark(a, node[a], (size_t)found);
         }
-        if (full && ++closed_since >= 64) {
-            open.erase(std::remove_if(open.begin(), open.end(),
-                                      [&](int32_t k) {
-                                          const St& T = st[(size_t)k];
-                                          return T.used[0] >= FULL || T.used[1] >= FULL || T.used[2] >= FULL;
-                                      }),
-                       open.end());
-            closed_since = 0;
-        }
+        if (full)
+            set_bit(closed, (size_t)found);
     }
-    quit.store(true, std::memory_order_release);
-    gen.fetch_add(1, std::memory_order_acq_rel);
-    for (auto& t : pool)
-        t.join();
     s.strata_off.assign(1, 0);
     s.strata_ids.clear();
     s.max_parallel_cf = 0;
