@@ -188,33 +188,58 @@ def cpu_sample(flat, tx, tv, w, budget_s, threads):
     return done_upd, done_t, g
 
 
+# The reference arm replays the reference update rule on a bounded sample of
+# the workload: the first REF_SAMPLE_NNZ cells of the same draw (same seed,
+# shape, index distributions, values, split and hyper-parameters), drawn,
+# shuffled (std::mt19937(42), main.cpp:303-306) and blocked
+# (block_problem, block.cu:1233-1287) by the oracle's restatements, so that
+# nothing of the product library is loaded.
+REF_SAMPLE_NNZ = 10_000_000
+
+
+def reference_sample(name):
+    import oracle
+
+    w = WORKLOADS[name]
+    m = min(w["nnz"], REF_SAMPLE_NNZ)
+    t0 = time.time()
+    tx, tv, sx, sv = oracle.gen_tensor(w["I"], w["J"], w["K"], m, zipf=w["zipf"], gt_rank=w["gt_rank"],
+                                       gt_std=0.5, noise_std=w["noise"], train_frac=w["train"], seed=SEED)
+    oracle.shuffle(tx, tv)
+    t1 = time.time()
+    sched = oracle.Schedule(tx, w["I"], w["J"], w["K"], 2048, 8)
+    t2 = time.time()
+    log("reference sample: %d cells (%d train), drawn %.1fs, blocked %.1fs: %d blocks, %d groups, %d slots"
+        % (m, len(tv), t1 - t0, t2 - t1, sched.nblocks, sched.ngroups, sched.nslots))
+    flat = oracle.FlatSchedule(sched.group_off, sched.slot_ids, sched.slot_coe,
+                               lambda b: sched.block_entries[b])
+    return w, m, tx, tv, sched, flat
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    import btc_gpu as bg
-
-    w, tx, tv, sx, sv, _ = build_workload(args.workload)
-    cfg = cfg_for(w, bg.F64, bg.HOGWILD)
-    cfg.resident_blocks = -1
-    sched = bg.Schedule(cfg, tx)
-    flat = flat_schedule(sched)
+    w, m, tx, tv, sched, flat = reference_sample(args.workload)
     threads = os.cpu_count() or 1
     per_step = max(min(2.0, args.ref_seconds), args.ref_seconds / max(1, args.steps + args.warmup))
     for _ in range(args.warmup):
         cpu_sample(flat, tx, tv, w, per_step / 4, threads)
     ups, times = [], []
+    g = 0
     for _ in range(args.steps):
         u, t, g = cpu_sample(flat, tx, tv, w, per_step, threads)
         ups.append(u)
         times.append(t)
     value = sum(ups) / sum(times)
-    sample = ("first %d of %d strata of one epoch per step (%.0f updates/step), FP64 Hogwild threads, "
-              "schedule identical to the reference's block_problem" % (g, sched.summary.num_groups, np.mean(ups)))
+    sample = ("first %d cells of the workload's draw (%d train entries, shuffled with std::mt19937(42)), blocked "
+              "by the oracle's restatement of block_problem (%d groups); per step the leading groups of an epoch "
+              "(%.0f updates on average, up to %d groups), FP64 Hogwild threads, barrier per group"
+              % (m, len(tv), sched.ngroups, np.mean(ups), g))
     line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "updates/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * np.mean(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": w["desc"]},
+            "data": "synthetic", "config": config_of(w, args.workload, "f64", "hogwild"),
             "cpu_baseline": {"value": value, "unit": "updates/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

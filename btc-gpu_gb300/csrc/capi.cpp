@@ -21,6 +21,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <limits>
 #include <new>
 #include <string>
@@ -83,6 +84,9 @@ struct btc_ctx {
     size_t st_smem = 0;
     std::vector<float> tile_feat;  // BTC_TILE_FEATURES per tile
     std::vector<int> h_tile0, h_ntiles;  // host copy of each slot's tiles
+    // per scheduled block (first use order): cost-model features and tiles
+    std::vector<int32_t> blk_ids, blk_tile0, blk_ntiles;
+    std::vector<float> blk_feat;
     unsigned* tile_ns = nullptr;   // device, allocated on the first profiled epoch
     bool profile_next = false;
     long long st_rows = 0, st_tiles = 0;
@@ -250,6 +254,52 @@ btc_status btc_schedule_build(const btc_config* cfg, const int32_t* xyz, int64_t
         return rc;
     }
     *out = s;
+    return BTC_OK;
+}
+
+btc_status btc_schedule_build_learned(const btc_config* cfg, const int32_t* xyz, int64_t n, btc_mlp* model,
+                                      btc_schedule** out)
+{
+    if (!cfg || !out || (n > 0 && !xyz))
+        return BTC_ERR_ARG;
+    *out = nullptr;
+    if (model) {
+        int64_t np = 0;
+        if (btc_mlp_param_count(model, &np) != BTC_OK || btc_mlp_inputs(model) != BTC_BLOCK_FEATURES)
+            return BTC_ERR_ARG;
+    }
+    btc_schedule* s = new (std::nothrow) btc_schedule();
+    if (!s)
+        return BTC_ERR_ALLOC;
+    std::function<bool(const float*, int64_t, float*)> predict;
+    if (model)
+        predict = [model](const float* x, int64_t m, float* y) { return btc_mlp_predict(model, x, m, y) == BTC_OK; };
+    btc_status rc;
+    try {
+        rc = btc::build_learned(*cfg, xyz, n, default_threads(*cfg), predict, s->s);
+    } catch (const std::bad_alloc&) {
+        rc = BTC_ERR_ALLOC;
+    }
+    if (rc != BTC_OK) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return BTC_OK;
+}
+
+btc_status btc_schedule_block_boxes(const btc_schedule* sp, int32_t* boxes)
+{
+    if (!sp || !boxes)
+        return BTC_ERR_ARG;
+    if (!sp->s.learned)
+        return BTC_ERR_STATE;
+    const auto& B = sp->s.blocks;
+    for (size_t i = 0; i < B.size(); i++)
+        for (int a = 0; a < 3; a++) {
+            boxes[6 * i + 2 * a] = B[i].lo[a];
+            boxes[6 * i + 2 * a + 1] = B[i].hi[a];
+        }
     return BTC_OK;
 }
 
@@ -541,6 +591,13 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
         c->st_rows = (long long)ts.rows.size();
         c->h_tile0 = t0;
         c->h_ntiles = tn;
+        btc::scheduled_block_features(s, txyz, default_threads(cfg), c->blk_ids, c->blk_feat);
+        c->blk_tile0.resize(c->blk_ids.size());
+        c->blk_ntiles.resize(c->blk_ids.size());
+        for (size_t i = 0; i < c->blk_ids.size(); i++) {
+            c->blk_tile0[i] = ts.block_tile0[(size_t)c->blk_ids[i]];
+            c->blk_ntiles[i] = ts.block_ntiles[(size_t)c->blk_ids[i]];
+        }
         c->tile_feat.assign(ts.tiles.size() * BTC_TILE_FEATURES, 0.f);
         for (size_t t = 0; t < ts.tiles.size(); t++) {
             const btc::TileHdr& h = ts.tiles[t];
@@ -1010,6 +1067,36 @@ btc_status btc_ctx_set_work_units(btc_ctx* c, const int32_t* unit_off, int32_t n
         return rc;
     CK(cudaStreamSynchronize(c->stream));
     c->nunits = nunits;
+    return BTC_OK;
+}
+
+btc_status btc_ctx_block_profile(btc_ctx* c, float* features, float* log_us, int64_t* n)
+{
+    if (!c || !n || c->mode != BTC_MODE_STAGED)
+        return BTC_ERR_ARG;
+    const int64_t nb = (int64_t)c->blk_ids.size();
+    if (*n < nb || (nb > 0 && (!features || !log_us))) {
+        *n = nb;
+        return BTC_ERR_ARG;
+    }
+    std::vector<uint32_t> ns((size_t)c->st_tiles);
+    btc_epoch_stats es{};
+    btc_status rc = btc_train_epoch_profiled(c, ns.data(), &es);
+    if (rc)
+        return rc;
+    int64_t k = 0;
+    for (int64_t i = 0; i < nb; i++) {
+        double t = 0;
+        for (int q = c->blk_tile0[(size_t)i]; q < c->blk_tile0[(size_t)i] + c->blk_ntiles[(size_t)i]; q++)
+            t += ns[(size_t)q] * 1e-3;
+        if (t <= 0)
+            continue;
+        std::copy(c->blk_feat.begin() + i * BTC_BLOCK_FEATURES, c->blk_feat.begin() + (i + 1) * BTC_BLOCK_FEATURES,
+                  features + k * BTC_BLOCK_FEATURES);
+        log_us[k] = (float)std::log(t);
+        k++;
+    }
+    *n = k;
     return BTC_OK;
 }
 

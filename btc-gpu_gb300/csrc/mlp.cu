@@ -384,6 +384,8 @@ btc_status btc_mlp_train(btc_mlp* m, const float* x, const float* y, int64_t n, 
     return rc;
 }
 
+int32_t btc_mlp_inputs(const btc_mlp* m) { return m ? (int32_t)m->L.nin : 0; }
+
 btc_status btc_mlp_predict(btc_mlp* m, const float* x, int64_t n, float* y)
 {
     if (!m || n < 0 || (n > 0 && (!x || !y)))

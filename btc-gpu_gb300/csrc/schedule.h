@@ -4,6 +4,7 @@
 // (block.cu:1233-1278) for the same input order.
 #pragma once
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -17,6 +18,9 @@ struct BlockRec {
     uint64_t lcode[3];  // the same bits left-aligned in 64 bits (for prefix tests)
     uint64_t bins[3];   // which of the 64 top-level intervals the block covers
     std::vector<int32_t> ent;  // entry indices in block order
+    // learned schedules: the block's box [lo, hi) per axis (no codes)
+    bool boxed = false;
+    int32_t lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
 };
 
 struct Schedule {
@@ -34,6 +38,7 @@ struct Schedule {
     int32_t global_levels[3] = {1, 1, 1};
     double seconds[3] = {0, 0, 0};
     int64_t scheduled_updates = 0;
+    bool learned = false;  // built by build_learned: boxes, no padding
 };
 
 // Builds the whole schedule.  Returns BTC_OK or an error status.
@@ -45,5 +50,14 @@ int32_t stratum_target(int32_t max_parallel, int32_t block_num, int32_t pss, int
 
 // block_parallel.txt text (block.cu:822-925).
 std::string report_text(const Schedule& s);
+
+// The learned schedule (learned.cpp): median splits on the axis a cost model
+// picks (`predict`: features -> log microseconds per block; empty = axes in
+// turn), every block scheduled once, conflict-free groups heaviest first.
+btc_status build_learned(const btc_config& cfg, const int32_t* xyz, int64_t n, int threads,
+                         const std::function<bool(const float*, int64_t, float*)>& predict, Schedule& out);
+// The 10 cost-model features of every scheduled block (first use order).
+void scheduled_block_features(const Schedule& s, const int32_t* xyz, int threads, std::vector<int32_t>& blocks,
+                              std::vector<float>& feat);
 
 }  // namespace btc

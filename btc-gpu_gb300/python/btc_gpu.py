@@ -16,6 +16,7 @@ CLI_PATH = os.path.join(PKG, "bin", "tensor_sgd")
 
 F32, F64, BF16 = 0, 1, 2
 NOALLOC_MAX_ENTRIES = 67108864
+BLOCK_FEATURES = 10
 TILE_FEATURES = 10
 HOGWILD, DETERMINISTIC, STAGED = 0, 1, 2
 TRAIN, TEST = 0, 1
@@ -87,6 +88,10 @@ SIGNATURES = {
     "btc_free": ([P], None),
     "btc_shuffle_entries": ([P, P, I64, U32], ctypes.c_int),
     "btc_schedule_build": ([P, P, I64, P], ctypes.c_int),
+    "btc_schedule_build_learned": ([P, P, I64, P, P], ctypes.c_int),
+    "btc_schedule_block_boxes": ([P, P], ctypes.c_int),
+    "btc_ctx_block_profile": ([P, P, P, ctypes.POINTER(I64)], ctypes.c_int),
+    "btc_mlp_inputs": ([P], I32),
     "btc_schedule_summarize": ([P, P], ctypes.c_int),
     "btc_schedule_blocks": ([P, P, P], ctypes.c_int),
     "btc_schedule_block_entries": ([P, I32, P, P], ctypes.c_int),
@@ -359,14 +364,23 @@ class PinnedArray:
 
 
 class Schedule:
-    """Host schedule: block_problem's blocking, strata and balancing."""
+    """Host schedule: block_problem's blocking, strata and balancing; with
+    learned=True the learned blocking (btc_schedule_build_learned) instead,
+    its split axes chosen by `model` (an MLP over BLOCK_FEATURES, or None for
+    the axes in turn)."""
 
-    def __init__(self, cfg, xyz):
+    def __init__(self, cfg, xyz, learned=False, model=None):
         self.cfg = cfg
+        self.learned = learned
         self.xyz = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1, 3)
         h = ctypes.c_void_p()
-        _ck(_lib().btc_schedule_build(ctypes.byref(cfg), _p(self.xyz), self.xyz.shape[0], ctypes.byref(h)),
-            "btc_schedule_build")
+        if learned:
+            _ck(_lib().btc_schedule_build_learned(ctypes.byref(cfg), _p(self.xyz), self.xyz.shape[0],
+                                                  model.handle if model is not None else None, ctypes.byref(h)),
+                "btc_schedule_build_learned")
+        else:
+            _ck(_lib().btc_schedule_build(ctypes.byref(cfg), _p(self.xyz), self.xyz.shape[0], ctypes.byref(h)),
+                "btc_schedule_build")
         self._h = h
         s = ScheduleSummary()
         _ck(_lib().btc_schedule_summarize(h, ctypes.byref(s)), "btc_schedule_summarize")
@@ -382,6 +396,12 @@ class Schedule:
         codes = np.zeros((n, 3), np.uint64)
         _ck(_lib().btc_schedule_blocks(self._h, _p(meta), _p(codes)), "btc_schedule_blocks")
         return meta, codes
+
+    def boxes(self):
+        """[lo, hi) per axis of every block of a learned schedule, (blocks, 3, 2)."""
+        out = np.zeros((self.summary.num_blocks, 3, 2), np.int32)
+        _ck(_lib().btc_schedule_block_boxes(self._h, _p(out)), "btc_schedule_block_boxes")
+        return out
 
     def block_entries(self, b):
         cap = ctypes.c_int32(self.cfg.block_s)
@@ -490,6 +510,16 @@ class Context:
         r = AutotuneReport()
         _ck(_lib().btc_ctx_autotune(self._h, epochs_per_candidate, ctypes.byref(r)), "btc_ctx_autotune")
         return r
+
+    def block_profile(self):
+        """(features, log microseconds) of every scheduled block, from one
+        profiled training epoch (the block cost model's training samples)."""
+        n = ctypes.c_int64(0)
+        _lib().btc_ctx_block_profile(self._h, None, None, ctypes.byref(n))
+        f = np.zeros((max(n.value, 1), BLOCK_FEATURES), np.float32)
+        y = np.zeros(max(n.value, 1), np.float32)
+        _ck(_lib().btc_ctx_block_profile(self._h, _p(f), _p(y), ctypes.byref(n)), "btc_ctx_block_profile")
+        return f[: n.value], y[: n.value]
 
     def train_epoch_profiled(self):
         n = ctypes.c_int64()

@@ -239,6 +239,33 @@ btc_status btc_mlp_gradient(btc_mlp *m, const float *x, const float *y, int64_t 
 btc_status btc_mlp_train(btc_mlp *m, const float *x, const float *y, int64_t n, int32_t steps, float lr,
                          double *final_loss);
 btc_status btc_mlp_predict(btc_mlp *m, const float *x, int64_t n, float *y);
+/* number of input features the model was created with */
+int32_t btc_mlp_inputs(const btc_mlp *m);
+
+/* ---- learned blocking -------------------------------------------------------
+ * No counterpart in the reference (which splits at code-range midpoints,
+ * block.cu:154-401, and pads strata with repeated blocks, block.cu:660-697).
+ * A binary tree over the (i, j, k) space whose leaves hold <= block_s
+ * entries, each node split at the median coordinate of its entries on the
+ * axis the cost model predicts cheapest (model: BTC_BLOCK_FEATURES inputs,
+ * log microseconds per block; NULL = the axes in turn); every block is
+ * scheduled once per epoch, in conflict-free groups of at most
+ * parallel_sequence_size blocks (8 when 0), heaviest predicted first; every
+ * coe weight is 1.  Not bit-exact with the reference by design: measured
+ * epoch time or time to a test RMSE decides between it and
+ * btc_schedule_build.  The schedule works with every context mode. */
+#define BTC_BLOCK_FEATURES 10
+btc_status btc_schedule_build_learned(const btc_config *cfg, const int32_t *xyz, int64_t n, btc_mlp *model,
+                                      btc_schedule **out);
+/* boxes[6*b ..] = lo_x, hi_x, lo_y, hi_y, lo_z, hi_z of block b (learned
+ * schedules only; BTC_ERR_STATE otherwise) */
+btc_status btc_schedule_block_boxes(const btc_schedule *s, int32_t *boxes);
+/* Training samples for the block cost model (staged contexts): one profiled
+ * training epoch, then for every scheduled block with a measured time its
+ * BTC_BLOCK_FEATURES features (entries, distinct rows and largest row share
+ * per mode, ...) and the log of its microseconds.  *n in: capacity (samples),
+ * out: samples written (or, with too small a capacity, the count needed). */
+btc_status btc_ctx_block_profile(btc_ctx *ctx, float *features, float *log_us, int64_t *n);
 
 typedef struct btc_learn_report {
     double plain_ms;      /* mean measured epoch time, one slot per unit */

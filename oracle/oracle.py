@@ -23,8 +23,9 @@ def _load():
     global _lib
     if _lib is not None:
         return _lib
-    if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(
-        os.path.join(_HERE, "btc_oracle.c")
+    srcs = ("btc_oracle.c", "gen.c", "shuffle.cpp")
+    if not os.path.exists(_LIB_PATH) or any(
+        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, f)) for f in srcs
     ):
         build()
     lib = ctypes.CDLL(_LIB_PATH)
@@ -53,6 +54,15 @@ def _load():
     lib.orc_sgd_replay_mt.restype = ctypes.c_int64
     lib.orc_hx_public.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
     lib.orc_hx_public.restype = ctypes.c_int
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    I64P = ctypes.POINTER(ctypes.c_int64)
+    lib.orc_gen_tensor.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int64, P, ctypes.c_int,
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                   PP, PP, I64P, PP, PP, I64P]
+    lib.orc_gen_tensor.restype = ctypes.c_int
+    lib.orc_gen_free.argtypes = [P]
+    lib.orc_shuffle.argtypes = [P, P, ctypes.c_int64, ctypes.c_uint32]
+    lib.orc_shuffle.restype = ctypes.c_int
     _lib = lib
     return lib
 
@@ -206,3 +216,38 @@ class FlatSchedule:
         return lib.orc_sgd_replay_mt(g0, g1, _ptr(self.goff), _ptr(self.soff), _ptr(self.ent),
                                      _ptr(self.coe), _ptr(xyz), _ptr(val), R, lr, reg, _ptr(A), _ptr(B),
                                      _ptr(C), threads)
+
+
+def gen_tensor(I, J, K, nnz, zipf=(0.0, 0.0, 0.0), gt_rank=8, gt_std=0.5, noise_std=0.01, train_frac=0.9,
+               seed=1):
+    """The benchmark's synthetic tensor drawn by the oracle's restatement of
+    the generator (gen.c): (train xyz, train values, test xyz, test values).
+    A draw of nnz = M cells is the first M cells of a larger draw."""
+    lib = _load()
+    zs = np.ascontiguousarray(zipf, dtype=np.float64)
+    ptrs = [ctypes.c_void_p() for _ in range(4)]
+    ntr, nte = ctypes.c_int64(), ctypes.c_int64()
+    rc = lib.orc_gen_tensor(I, J, K, nnz, _ptr(zs), gt_rank, gt_std, noise_std, train_frac, seed,
+                            ctypes.byref(ptrs[0]), ctypes.byref(ptrs[1]), ctypes.byref(ntr),
+                            ctypes.byref(ptrs[2]), ctypes.byref(ptrs[3]), ctypes.byref(nte))
+    if rc != 0:
+        raise RuntimeError("oracle generator failed with status %d" % rc)
+
+    def take(p, n, dt, width):
+        out = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(dt)), shape=(max(n * width, 1),))[: n * width].copy()
+        lib.orc_gen_free(p)
+        return out.reshape(n, width) if width > 1 else out
+
+    tx = take(ptrs[0], ntr.value, ctypes.c_int32, 3)
+    tv = take(ptrs[1], ntr.value, ctypes.c_double, 1)
+    sx = take(ptrs[2], nte.value, ctypes.c_int32, 3)
+    sv = take(ptrs[3], nte.value, ctypes.c_double, 1)
+    return tx, tv, sx, sv
+
+
+def shuffle(xyz, val, seed=42):
+    """main.cpp:303-306: std::shuffle with std::mt19937(seed), in place."""
+    lib = _load()
+    assert xyz.dtype == np.int32 and xyz.flags.c_contiguous and val.dtype == np.float64 and val.flags.c_contiguous
+    lib.orc_shuffle(_ptr(xyz), _ptr(val), len(val), seed)
+    return xyz, val

@@ -116,3 +116,28 @@ def test_hx_float_rounding():
             if oracle.hx(I, level, num) != exact:
                 diffs += 1
     assert diffs > 0
+
+
+@pytest.mark.parametrize("spec", [dict(I=500, J=400, K=300, nnz=20000, zipf=(1.2, 1.2, 1.2), gt_rank=4, seed=3),
+                                  dict(I=2000, J=300, K=90000, nnz=100000, zipf=(1.5, 0.0, 1.5), gt_rank=0,
+                                       noise_std=0.0, seed=4),
+                                  dict(I=100000, J=100000, K=10000, nnz=200000, zipf=(1.3, 1.3, 1.3), gt_rank=32,
+                                       noise_std=0.05, train_frac=0.95, seed=20261208)])
+def test_oracle_generator_and_shuffle_equal_the_library(spec):
+    """The reference arm draws its sample with the oracle's generator and
+    shuffles it with the oracle's std::mt19937 shuffle, never loading the
+    product library; both must give exactly the library's entries, and a
+    draw of fewer cells must be a prefix of a larger draw."""
+    import btc_gpu as bg
+
+    got = oracle.gen_tensor(**spec)
+    want = bg.gen_tensor(**spec)
+    for a, b in zip(got, want):
+        assert a.dtype == b.dtype and np.array_equal(a, b)
+    small = oracle.gen_tensor(**dict(spec, nnz=spec["nnz"] // 2))
+    if spec.get("gt_rank", 8) > 0:  # log-normal values are rescaled by each draw's own maximum
+        for a, b in ((small[0], got[0]), (small[1], got[1])):
+            assert np.array_equal(a, b[: len(a)])
+    tx, tv = oracle.shuffle(got[0].copy(), got[1].copy())
+    ux, uv = bg.shuffle(want[0].copy(), want[1].copy())
+    assert np.array_equal(tx, ux) and np.array_equal(tv, uv)
