@@ -1,28 +1,45 @@
 #!/usr/bin/env python3
-"""Throughput of one CP-SGD epoch on one GB300 (nnz-updates/s).
+"""Throughput and time-to-RMSE of CP-SGD epochs on one GB300.
 
-Workload (default, "c2"): the skewed medium tensor -- I = J = 100,000,
-K = 10,000, 50M unique entries with every mode's index Zipf(1.2), values from
-a rank-16 ground-truth CP (factors N(0, 0.5)) plus N(0, 0.05) noise, 90/10
-train/test split, rank R = 32, lr 0.005, lambda 0.02, factors U(0, 0.1).
-Data are seeded synthetic stand-ins generated in memory; the schedule is the
-reference's blocking (block_s 2048, 8 blocks per stratum).
+Workload (default, "c5"): the largest single tensor -- I = J = 1M, K = 100k,
+1B unique entries with every mode's index Zipf(1.3), values from a rank-32
+ground-truth CP (factors N(0, 0.5)) plus N(0, 0.05) noise, 95/5 train/test
+split, rank R = 32, lr 0.005, lambda 0.02, factors U(0, 0.1).  Data are
+seeded synthetic stand-ins generated in memory; no public dataset is
+involved.  --workload c2 / c3 / c1 / small / c4 select the other shapes.
 
-A step is one epoch: every scheduled slot's entries updated once.
-  value      updates/s of the epoch kernels with everything resident in HBM,
-             timed with CUDA events on the launching stream (K epochs
-             back to back, warm-up W epochs first)
+Paths:
+  tuned   the chosen form: BF16 factors (stochastic rounding, FP32 masters of
+          hot rows), the staged kernel, autotuned, on the learned blocking
+          (median splits on axes a block cost model picks, every block once
+          per epoch); the model is trained on block timings recorded by a
+          profiled epoch on the reference blocking, and measured epoch time
+          decides between the two blockings (the reference's is the fallback)
+  plain   FP32 on the reference's blocking (block_problem, bit-exact) with
+          the reference kernel's execution model (Hogwild)
+
+A step is one epoch of the tuned path.
+  value      executed updates/s of the tuned epochs with everything resident in
+             HBM, CUDA events on the launching stream (K epochs back to back
+             after W warm-up epochs)
   e2e        the same metric through the C ABI's host-buffer call
              (btc_train_epoch_host): factors uploaded from pinned host
              memory, one epoch, test metrics, factors read back
-  roofline   algorithmic bytes per update (12 index + 4 value + 6*R*4 row
+  roofline   algorithmic bytes per update (12 index + 4 value + 6*R*2 row
              bytes) x updates / kernel time, against the measured HBM copy
              bandwidth
+  time_to_rmse  per-epoch test and train RMSE of both paths from the same
+             init, in the configured regime and in a learning regime (the
+             reference's default lambda 0.0005), and the device time each
+             path needs to reach 1.01 x the plain path's final test RMSE
+  oracle_check  factors after one epoch on the workload's first 10M cells
+             against the serial FP64 replay of the same schedule
   cpu_baseline  the reference update rule replayed serially (FP64) on one
-             host core over a bounded sample of the same schedule
+             host core over a bounded sample of the reference schedule
 
 --impl reference times the reference's update rule replayed on all host
-cores (Hogwild threads, FP64) on a bounded sample of the same schedule.
+cores (Hogwild threads, FP64) on a bounded sample drawn, shuffled and
+blocked by the oracle (no product library is loaded).
 
 Multi-GPU: the path does not shard (a single tensor's schedule is serial
 between strata); --gpus N under torchrun runs N independent replicas
@@ -64,6 +81,12 @@ WORKLOADS = {
                   desc="small skewed: I=J=20k K=5k, 2M nnz Zipf(1.2), R=32"),
 }
 METRIC = "nnz-updates/s & time-to-test-RMSE, tuned vs plain FP32, 1×GB300, % HBM peak"
+# the learning regime: the reference's default hyper-parameters
+# (tensor_SGD.cu:24-41: lr 0.005, reg 0.0005); the configured lambdas keep the
+# factors near the zero model, where the test RMSE hardly moves
+LEARN = dict(lr=0.005, reg=0.0005)
+# epochs of the time-to-RMSE trajectories (configured regime, learning regime)
+TRAJ_EPOCHS = {"c5": (8, 30), "c3": (10, 40), "c2": (20, 60), "c1": (10, 60), "small": (10, 60)}
 SEED = 20261203 + 1
 CTAS = 0
 # DRAM bytes per launch of the timed kernel from an ncu capture of the same
@@ -136,6 +159,11 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def config_of(w, name):
+    """The config object both arms print (the driver compares them)."""
+    return {"workload": w["desc"], "name": name}
+
+
 def build_workload(name, rank0=True):
     import btc_gpu as bg
 
@@ -153,6 +181,20 @@ def cfg_for(w, dtype, mode, device=0):
 
     return bg.config(I=w["I"], J=w["J"], K=w["K"], rank=w["R"], lr=w["lr"], reg=w["reg"], block_s=2048,
                      parallel_sequence_size=8, dtype=dtype, mode=mode, device=device, ctas_per_sm=CTAS)
+
+
+class Phases:
+    """Wall time of the set-up phases (logged, and reported in the line)."""
+
+    def __init__(self):
+        self.t = time.time()
+        self.d = {}
+
+    def mark(self, name):
+        now = time.time()
+        self.d[name] = round(now - self.t, 2)
+        log("phase %-22s %7.1fs" % (name, now - self.t))
+        self.t = now
 
 
 def flat_schedule(sched, max_updates=250_000_000):
@@ -239,7 +281,7 @@ def run_reference(args):
     line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "updates/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * np.mean(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": config_of(w, args.workload, "f64", "hogwild"),
+            "data": "synthetic", "config": config_of(w, args.workload),
             "cpu_baseline": {"value": value, "unit": "updates/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -266,26 +308,92 @@ def _timed(ctx, steps, dist):
     return st, _max_over_ranks(st.kernel_ms, dist)
 
 
-def _trajectory(ctx, w, epochs):
-    """Fresh init, then per-epoch (cumulative device ms, test RMSE)."""
+def _trajectory(ctx, w, epochs, rates=None, train_every=1):
+    """Fresh init, then per epoch (epoch, cumulative device ms, test RMSE,
+    train RMSE or None)."""
     import btc_gpu as bg
 
     init = init_factors(w)
     for m in range(3):
         ctx.set_factors(m, init[m])
+    lr, reg = rates if rates else (w["lr"], w["reg"])
+    ctx.set_rates(lr, reg)
     t, out = 0.0, []
-    for _ in range(epochs):
+    for e in range(epochs):
         st = ctx.train_epoch()
         t += st.kernel_ms
-        out.append((t, ctx.eval(bg.TEST).rmse))
+        tr = ctx.eval(bg.TRAIN).rmse if (e + 1) % train_every == 0 or e + 1 == epochs else None
+        out.append((e + 1, round(t, 3), ctx.eval(bg.TEST).rmse, tr))
+    ctx.set_rates(w["lr"], w["reg"])
     return out
 
 
 def _time_to(traj, target):
-    for t, r in traj:
+    for e, t, r, _ in traj:
         if r <= target:
-            return t
-    return None
+            return e, t
+    return None, None
+
+
+def _ttr(traj_t, traj_p):
+    """Time (device ms) and epochs each path needs to reach 1.01 x the plain
+    path's final test RMSE."""
+    target = traj_p[-1][2] * 1.01
+    et, tt = _time_to(traj_t, target)
+    ep, tp = _time_to(traj_p, target)
+    first = traj_p[0][2]
+    return {"target": target, "tuned_ms": tt, "tuned_epochs": et, "plain_ms": tp, "plain_epochs": ep,
+            "speedup": (tp / tt) if (tt and tp) else None,
+            "tuned_final_rmse": traj_t[-1][2], "plain_final_rmse": traj_p[-1][2],
+            "tuned_vs_plain_rmse_rel": (traj_t[-1][2] - traj_p[-1][2]) / traj_p[-1][2],
+            "plain_rmse_moved_rel": (first - traj_p[-1][2]) / first,
+            "tuned": [[e, t, round(r, 6), None if tr is None else round(tr, 6)] for e, t, r, tr in traj_t],
+            "plain": [[e, t, round(r, 6), None if tr is None else round(tr, 6)] for e, t, r, tr in traj_p]}
+
+
+def _epoch_ms(ctx, n):
+    return ctx.train_epochs(n).kernel_ms / n
+
+
+def oracle_check(w, name, model, tuned_learned, dtype):
+    """One epoch of the tuned and the plain configuration on the workload's
+    first REF_SAMPLE_NNZ cells against the serial FP64 replay of the same
+    schedule (sgd_Kernel.cu:336-351); factor deviation and slope per mode
+    (factor_check.py), BF16 residual in ulps."""
+    import btc_gpu as bg
+    import oracle
+    from factor_check import agreement, bf16_ulp_residual
+
+    m = min(w["nnz"], REF_SAMPLE_NNZ)
+    tx, tv, sx, sv = bg.gen_tensor(w["I"], w["J"], w["K"], m, zipf=w["zipf"], gt_rank=w["gt_rank"], gt_std=0.5,
+                                   noise_std=w["noise"], train_frac=w["train"], seed=SEED)
+    bg.shuffle(tx, tv)
+    out = {"sample": "first %d cells of the workload (%d train entries), lr %g, lambda %g" % (m, len(tv), w["lr"],
+                                                                                              w["reg"])}
+    rng = np.random.default_rng(SEED + 9)
+    init = [rng.uniform(0.0, 0.1, (n, w["R"])) for n in (w["I"], w["J"], w["K"])]
+    for key, dt, md, learned in (("tuned", dtype, bg.STAGED, tuned_learned), ("plain", bg.F32, bg.HOGWILD, False)):
+        cfg = cfg_for(w, dt, md)
+        sched = bg.Schedule(cfg, tx, learned=learned, model=model if learned else None)
+        ctx = bg.Context(cfg, sched, tx, tv, sx, sv)
+        for q in range(3):
+            ctx.set_factors(q, init[q])
+        f0 = [ctx.get_factors(q) for q in range(3)]
+        ctx.train_epoch()
+        got = [ctx.get_factors(q) for q in range(3)]
+        ctx.close()
+        off, ids, coe = sched.groups()
+        flat = oracle.FlatSchedule(off, ids, coe, sched.block_entries)
+        ref = [a.copy() for a in f0]
+        flat.replay(tx, tv, w["R"], w["lr"], w["reg"], *ref)
+        ag = agreement(got, ref, f0)
+        out[key] = {"blocking": "learned" if learned else "reference", "dtype": {bg.F32: "f32", bg.BF16: "bf16",
+                                                                                 bg.F64: "f64"}[dt],
+                    "deviation": [round(d, 4) for d, _ in ag], "slope": [round(b, 4) for _, b in ag]}
+        if dt == bg.BF16:
+            out[key]["bf16_ulp_rms"] = round(bf16_ulp_residual(got, ref), 3)
+        sched.close()
+    return out
 
 
 def run_gpu(args):
@@ -302,35 +410,70 @@ def run_gpu(args):
         dist.init_process_group("gloo")
     dtype = {"f32": bg.F32, "f64": bg.F64, "bf16": bg.BF16}[args.dtype]
     mode = {"hogwild": bg.HOGWILD, "deterministic": bg.DETERMINISTIC, "staged": bg.STAGED}[args.mode]
-
+    ph = Phases()
     w, tx, tv, sx, sv, tgen = build_workload(args.workload)
+    ph.mark("generate+shuffle")
     cfg = cfg_for(w, dtype, mode, device=local)
-    t = time.time()
-    sched = bg.Schedule(cfg, tx)
-    tsched = time.time() - t
-    sm = sched.summary
-    log("workload %s: train %d test %d, gen %.1fs schedule %.1fs; blocks %d strata %d groups %d slots %d "
-        "updates/epoch %d" % (args.workload, len(tv), len(sv), tgen, tsched, sm.num_blocks, sm.num_strata,
-                              sm.num_groups, sm.num_slots, sm.scheduled_updates))
-    upd_per_step = sm.scheduled_updates
+    sched_h = bg.Schedule(cfg, tx)
+    ph.mark("schedule_reference")
+    sm = sched_h.summary
+    log("workload %s: train %d test %d; reference blocking: blocks %d strata %d groups %d slots %d updates/epoch %d "
+        "(blocking %.1fs strata %.1fs balance %.1fs)" % (args.workload, len(tv), len(sv), sm.num_blocks,
+                                                          sm.num_strata, sm.num_groups, sm.num_slots,
+                                                          sm.scheduled_updates, *sm.build_seconds))
     init = init_factors(w)
 
-    # the tuned path: staged kernel, chosen precision, autotuned, learned work units
-    ctx = bg.Context(cfg, sched, tx, tv, sx, sv)
-    for m in range(3):
-        ctx.set_factors(m, init[m])
+    def ctx_on(sched, dt, md):
+        c = bg.Context(cfg_for(w, dt, md, device=local), sched, tx, tv, sx, sv)
+        for q in range(3):
+            c.set_factors(q, init[q])
+        return c
+
+    # the tuned path: staged kernel in the chosen precision, autotuned, on the
+    # learned blocking when it is faster than the reference's
+    learned = None
+    model = None
+    tune = None
+    ctx = ctx_on(sched_h, dtype, mode)
+    sched = sched_h
+    ph.mark("context_tuned_reference")
     ctx.train_epochs(args.warmup)
-    tune = learn = None
     if mode == bg.STAGED and not args.no_tune:
         tune = ctx.autotune(2)
-        model = bg.MLP()
-        learn = ctx.learn_work_units(model, train_steps=300, trial_epochs=2)
-        model.close()
-        log("autotune: G=%d NV=%d ctas/SM=%d (%d candidates) %.3f -> %.3f ms; learned units: %d, R2 %.3f, "
-            "plain %.3f ms learned %.3f ms kept %d" % (tune.lanes_per_entry, tune.vectors_per_lane,
-                                                       tune.ctas_per_sm, tune.candidates, tune.default_ms,
-                                                       tune.best_ms, learn.units, learn.model_r2, learn.plain_ms,
-                                                       learn.learned_ms, learn.kept))
+        ph.mark("autotune")
+    if mode == bg.STAGED and not args.no_learned:
+        ms_h = _epoch_ms(ctx, 3)
+        f, y = ctx.block_profile()
+        model = bg.MLP(n_in=bg.BLOCK_FEATURES, seed=7)
+        loss = model.train(f, y, 400)
+        r2 = 1.0 - loss / max(1e-12, float(np.var(y)))
+        ph.mark("block_profile+model")
+        sched_l = bg.Schedule(cfg, tx, learned=True, model=model)
+        ph.mark("schedule_learned")
+        ctx_l = ctx_on(sched_l, dtype, mode)
+        ph.mark("context_tuned_learned")
+        ctx_l.train_epochs(args.warmup)
+        tune_l = ctx_l.autotune(2) if not args.no_tune else None
+        ms_l = _epoch_ms(ctx_l, 3)
+        upd_l, upd_h = sched_l.summary.scheduled_updates, sm.scheduled_updates
+        kept = ms_l < ms_h
+        learned = {"kept": bool(kept), "model_r2": r2, "samples": int(len(y)),
+                   "epoch_ms_learned": ms_l, "epoch_ms_reference": ms_h,
+                   "updates_per_epoch_learned": int(upd_l), "updates_per_epoch_reference": int(upd_h),
+                   "blocks_learned": int(sched_l.summary.num_blocks), "groups_learned": int(sched_l.summary.num_groups),
+                   "build_seconds_learned": round(sum(sched_l.summary.build_seconds), 2)}
+        log("learned blocking: %d blocks, %d groups, %d updates/epoch, %.3f ms/epoch vs reference %.3f ms/epoch "
+            "(%d updates); model R2 %.3f on %d blocks; kept %d" % (sched_l.summary.num_blocks,
+                                                                   sched_l.summary.num_groups, upd_l, ms_l, ms_h,
+                                                                   upd_h, r2, len(y), kept))
+        if kept:
+            ctx.close()
+            ctx, sched, tune = ctx_l, sched_l, tune_l
+        else:
+            ctx_l.close()
+            sched_l.close()
+        ph.mark("judge")
+    upd_per_step = sched.summary.scheduled_updates
     rm0 = ctx.eval(bg.TEST).rmse
     clocks = Clocks(local)
     clocks.start()
@@ -338,6 +481,7 @@ def run_gpu(args):
     clk = clocks.stop()
     value = upd_per_step * args.steps * world / (ms / 1000.0)
     rm1 = ctx.eval(bg.TEST).rmse
+    ph.mark("timed")
 
     # end to end through the host-buffer call
     shapes = [(n, w["R"]) for n in (w["I"], w["J"], w["K"])]
@@ -355,32 +499,35 @@ def run_gpu(args):
     fac_bytes = sum(n * w["R"] * 8 for n in (w["I"], w["J"], w["K"]))
     e2e = {"value": upd_per_step * e2e_steps * world / e2e_s, "unit": "updates/s",
            "h2d_bytes_per_step": fac_bytes, "d2h_bytes_per_step": fac_bytes + 24}
-    traj_tuned = _trajectory(ctx, w, w["epochs"]) if not args.no_plain else None
     for p_ in pinned:
         p_.free()
+    ph.mark("e2e")
+    ecfg, elearn = TRAJ_EPOCHS.get(args.workload, (10, 30))
+    if args.traj_epochs:
+        ecfg, elearn = args.traj_epochs
+    traj_t = traj_tl = None
+    if not args.no_plain:
+        traj_t = _trajectory(ctx, w, ecfg)
+        traj_tl = _trajectory(ctx, w, elearn, rates=(LEARN["lr"], LEARN["reg"]), train_every=5)
+        ph.mark("trajectories_tuned")
     ctx.close()
 
     # the plain FP32 path (the reference kernel's execution model on every SM)
-    # and, for context, the staged FP32 kernel untuned
-    plain = staged32 = None
-    traj_plain = None
+    # on the reference's blocking
+    plain = None
+    traj_p = traj_pl = None
     if not args.no_plain:
-        for name, (dt_, md_) in (("plain", (bg.F32, bg.HOGWILD)), ("staged32", (bg.F32, bg.STAGED))):
-            if name == "staged32" and args.no_staged32:
-                continue
-            c2 = bg.Context(cfg_for(w, dt_, md_, device=local), sched, tx, tv, sx, sv)
-            for m in range(3):
-                c2.set_factors(m, init[m])
-            c2.train_epochs(args.warmup)
-            st2, ms2 = _timed(c2, args.steps, dist)
-            res = {"value": upd_per_step * args.steps * world / (ms2 / 1000.0), "ms_per_step": ms2 / args.steps,
-                   "dtype": "f32", "mode": "hogwild" if md_ == bg.HOGWILD else "staged"}
-            if name == "plain":
-                traj_plain = _trajectory(c2, w, w["epochs"])
-                plain = res
-            else:
-                staged32 = res
-            c2.close()
+        c2 = ctx_on(sched_h, bg.F32, bg.HOGWILD)
+        ph.mark("context_plain")
+        c2.train_epochs(args.warmup)
+        st2, ms2 = _timed(c2, args.steps, dist)
+        plain = {"value": sm.scheduled_updates * args.steps * world / (ms2 / 1000.0),
+                 "ms_per_step": ms2 / args.steps, "dtype": "f32", "mode": "hogwild", "blocking": "reference",
+                 "updates_per_epoch": int(sm.scheduled_updates)}
+        traj_p = _trajectory(c2, w, ecfg)
+        traj_pl = _trajectory(c2, w, elearn, rates=(LEARN["lr"], LEARN["reg"]), train_every=5)
+        c2.close()
+        ph.mark("plain")
 
     peak, src = peaks()
     s_f = {"f32": 4, "f64": 8, "bf16": 2}[args.dtype]
@@ -393,25 +540,32 @@ def run_gpu(args):
                 "traffic": TRAFFIC.get((args.workload, args.dtype, args.mode)), "peak_source": src,
                 "bytes_per_update": b_upd, "kernel": kern,
                 "note": "algorithmic bytes (indices, value, three rows read and written per update); factor rows "
-                        "stay in L2, so DRAM traffic (ncu, 'traffic') is far lower"}
+                        "are served from L2 and shared memory, so DRAM traffic (ncu, 'traffic') is far lower"}
 
     line = None
     if rank == 0:
-        flat = flat_schedule(sched)
+        check = None
+        if not args.no_check:
+            check = oracle_check(w, args.workload, model, bool(learned and learned["kept"]), dtype)
+            ph.mark("oracle_check")
+        flat = flat_schedule(sched_h)
         u, tcpu, g = cpu_sample(flat, tx, tv, w, args.cpu_seconds, 1)
         cpu = {"value": u / tcpu, "unit": "updates/s", "cores": 1, "kind": "port",
-               "sample": "first %d of %d strata of one epoch (%d updates), serial FP64 replay of the "
-                         "reference update rule" % (g, sm.num_groups, u)}
+               "sample": "first %d of %d groups of one epoch of the reference schedule (%d updates), serial FP64 "
+                         "replay of the reference update rule" % (g, sm.num_groups, u)}
+        ph.mark("cpu_baseline")
         line = {"metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
-                "config": {"workload": w["desc"], "precision": args.dtype, "mode": args.mode,
-                           "train_nnz": int(len(tv)), "updates_per_epoch": int(upd_per_step),
-                           "parallelism": "replicas" if world > 1 else "single",
-                           "l2": "inputs larger than L2: entry stream %.2f GB per epoch; factor rows "
-                                 "(%.0f MB) stay L2-resident as in a real run" %
-                                 (upd_per_step * 16 / 1e9, sum(n * w["R"] * s_f for n in
-                                                             (w["I"], w["J"], w["K"])) / 1e6)},
+                "config": config_of(w, args.workload),
+                "setup": {"precision": args.dtype, "mode": args.mode,
+                          "blocking": "learned" if (learned and learned["kept"]) else "reference",
+                          "train_nnz": int(len(tv)), "updates_per_epoch": int(upd_per_step),
+                          "parallelism": "replicas" if world > 1 else "single",
+                          "l2": "inputs larger than L2: entry stream %.2f GB per epoch; factor rows (%.0f MB) stay "
+                                "L2-resident as in a real run" % (upd_per_step * 16 / 1e9, sum(
+                                    n * w["R"] * s_f for n in (w["I"], w["J"], w["K"])) / 1e6),
+                          "phases_s": ph.d},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": st.launches,
                 "train_nnz_per_s": len(tv) * args.steps * world / (ms / 1000.0),
                 "test_rmse": {"after_warmup": rm0, "after_timed": rm1, "e2e_last": met.rmse}}
@@ -419,22 +573,19 @@ def run_gpu(args):
             line["autotune"] = {"lanes_per_entry": tune.lanes_per_entry, "vectors_per_lane": tune.vectors_per_lane,
                                 "ctas_per_sm": tune.ctas_per_sm, "candidates": tune.candidates,
                                 "default_ms": tune.default_ms, "best_ms": tune.best_ms}
-            line["learned_work_units"] = {"units": learn.units, "model_r2": learn.model_r2,
-                                          "samples": learn.samples, "plain_ms": learn.plain_ms,
-                                          "learned_ms": learn.learned_ms, "kept": bool(learn.kept)}
+        if learned is not None:
+            line["learned_blocking"] = learned
         if plain is not None:
             line["plain_fp32"] = plain
-            line["staged_fp32_untuned"] = staged32
-            target = traj_plain[-1][1] * 1.01
-            tt, tp = _time_to(traj_tuned, target), _time_to(traj_plain, target)
-            line["time_to_rmse"] = {
-                "target": target, "epochs": w["epochs"], "tuned_ms": tt, "plain_ms": tp,
-                "speedup": (tp / tt) if (tt and tp) else None,
-                "tuned_final_rmse": traj_tuned[-1][1], "plain_final_rmse": traj_plain[-1][1],
-                "tuned_vs_plain_rmse_rel": abs(traj_tuned[-1][1] - traj_plain[-1][1]) / traj_plain[-1][1]}
+            line["time_to_rmse"] = {"configured": dict(_ttr(traj_t, traj_p), lr=w["lr"], reg=w["reg"]),
+                                    "learning": dict(_ttr(traj_tl, traj_pl), **LEARN)}
+        if check is not None:
+            line["oracle_check"] = check
         if clk:
             line["clocks"] = clk
         print(json.dumps(line), flush=True)
+    if model is not None:
+        model.close()
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -532,10 +683,10 @@ def run_c4(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c4"])
+    ap.add_argument("--workload", default="c5", choices=sorted(WORKLOADS) + ["c4"])
     ap.add_argument("--dtype", default="bf16", choices=["f32", "f64", "bf16"])
     ap.add_argument("--mode", default="staged", choices=["hogwild", "deterministic", "staged"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -544,12 +695,15 @@ def main():
     ap.add_argument("--ctas", type=int, default=0, help="staged kernel CTAs per SM (0 = auto)")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner and the learned work units")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison")
-    ap.add_argument("--no-staged32", action="store_true",
-                    help="skip the untuned staged FP32 comparison (one context build less on large tensors)")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned blocking")
+    ap.add_argument("--no-check", action="store_true", help="skip the factor check against the oracle")
+    ap.add_argument("--traj-epochs", type=int, nargs=2, default=None,
+                    help="epochs of the configured-regime and learning-regime trajectories")
     args = ap.parse_args()
     global CTAS
     CTAS = args.ctas
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "c4":

@@ -93,6 +93,7 @@ struct btc_ctx {
     int64_t updates = 0;
     int nslots = 0;
     bool failed = false;
+    std::vector<double> coe_host;  // the schedule's coe weights, 3 per slot (without lr)
 };
 
 namespace {
@@ -522,6 +523,7 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
             items.push_back(make_int2(k, st));
     }
     c->nitems = (long long)items.size();
+    c->coe_host.assign(s.slot_coe.begin(), s.slot_coe.end());
     btc_status rc;
     if ((rc = upload((void**)&c->coo, coo.data(), coo.size() * sizeof(int4), c->stream)))
         return rc;
@@ -849,6 +851,30 @@ btc_status btc_ctx_create(const btc_config* cfg, const btc_schedule* s, const in
 }
 
 void* btc_ctx_stream(btc_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+btc_status btc_ctx_set_rates(btc_ctx* c, double lr, double reg)
+{
+    if (!c || !(lr > 0) || !(reg >= 0))
+        return BTC_ERR_ARG;
+    CK(cudaSetDevice(c->cfg.device));
+    const size_t n = c->coe_host.size();
+    if (c->dtype == BTC_DTYPE_F64) {
+        std::vector<double> v(n);
+        for (size_t i = 0; i < n; i++)
+            v[i] = c->coe_host[i] * lr;
+        CK(cudaMemcpyAsync(c->slot_coe, v.data(), n * 8, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    } else {
+        std::vector<float> v(n);
+        for (size_t i = 0; i < n; i++)
+            v[i] = (float)(c->coe_host[i] * lr);
+        CK(cudaMemcpyAsync(c->slot_coe, v.data(), n * 4, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    c->cfg.lr = lr;
+    c->cfg.reg = reg;
+    return BTC_OK;
+}
 
 btc_status btc_ctx_set_factors(btc_ctx* c, int32_t mode, const double* host)
 {

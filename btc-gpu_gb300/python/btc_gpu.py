@@ -92,6 +92,7 @@ SIGNATURES = {
     "btc_schedule_block_boxes": ([P, P], ctypes.c_int),
     "btc_ctx_block_profile": ([P, P, P, ctypes.POINTER(I64)], ctypes.c_int),
     "btc_mlp_inputs": ([P], I32),
+    "btc_ctx_set_rates": ([P, ctypes.c_double, ctypes.c_double], ctypes.c_int),
     "btc_schedule_summarize": ([P, P], ctypes.c_int),
     "btc_schedule_blocks": ([P, P, P], ctypes.c_int),
     "btc_schedule_block_entries": ([P, I32, P, P], ctypes.c_int),
@@ -510,6 +511,9 @@ class Context:
         r = AutotuneReport()
         _ck(_lib().btc_ctx_autotune(self._h, epochs_per_candidate, ctypes.byref(r)), "btc_ctx_autotune")
         return r
+
+    def set_rates(self, lr, reg):
+        _ck(_lib().btc_ctx_set_rates(self._h, lr, reg), "btc_ctx_set_rates")
 
     def block_profile(self):
         """(features, log microseconds) of every scheduled block, from one

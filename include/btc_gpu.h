@@ -188,6 +188,11 @@ btc_status btc_ctx_create(const btc_config *cfg, const btc_schedule *s, const in
 /* mode 0 = A (I rows), 1 = B (J rows), 2 = C (K rows); host is [rows][rank] */
 btc_status btc_ctx_set_factors(btc_ctx *ctx, int32_t mode, const double *host);
 btc_status btc_ctx_get_factors(btc_ctx *ctx, int32_t mode, double *host);
+/* New learning rate and regularisation for the following epochs (no
+ * counterpart in the reference, whose lr and reg are fixed per run).  The
+ * rows that decay from their value at write time stay the ones chosen at
+ * creation. */
+btc_status btc_ctx_set_rates(btc_ctx *ctx, double lr, double reg);
 /* U(lo, hi) init from a counter-based generator (seed, mode, row, col) */
 btc_status btc_ctx_init_factors(btc_ctx *ctx, uint64_t seed, double lo, double hi);
 /* One epoch: the reference's GPUs<<<max_parallel, thread_size>>> launch

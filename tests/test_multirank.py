@@ -79,3 +79,21 @@ def test_reference_arm_runs_on_rank_zero_only_under_torchrun():
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_reference_arm_does_not_load_the_product_library():
+    """The reference arm draws, shuffles and blocks its sample with oracle
+    code and replays it with the oracle: the process never maps the product
+    library."""
+    code = ("import sys; sys.path[:0] = [%r, %r]; import bench; "
+            "w, m, tx, tv, sched, flat = bench.reference_sample('small'); "
+            "u, t, g = bench.cpu_sample(flat, tx, tv, w, 0.5, 2); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('LOADED', 'libbtcgpu' in maps, 'ORACLE', 'libbtc_oracle' in maps, 'UPDATES', u)"
+            % (ROOT, os.path.join(ROOT, "oracle")))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-3000:]
+    out = r.stdout.split()
+    assert out[out.index("LOADED") + 1] == "False"
+    assert out[out.index("ORACLE") + 1] == "True"
+    assert int(out[out.index("UPDATES") + 1]) > 0
