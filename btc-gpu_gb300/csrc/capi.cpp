@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -161,6 +162,20 @@ bool coords_in_range(const int32_t* xyz, int64_t n, int32_t I, int32_t J, int32_
     for (auto& th : pool)
         th.join();
     return std::all_of(ok.begin(), ok.end(), [](char v) { return v != 0; });
+}
+
+// fn(lo, hi) over [0, n) split into contiguous shares on up to `threads`
+// host threads (one share below `serial_below` items)
+void parallel_for(int64_t n, int threads, const std::function<void(int64_t, int64_t)>& fn,
+                  int64_t serial_below = 1 << 16)
+{
+    const int T = n < serial_below ? 1 : std::max(1, std::min(threads, 64));
+    std::vector<std::thread> pool;
+    for (int t = 1; t < T; t++)
+        pool.emplace_back(fn, n * t / T, n * (t + 1) / T);
+    fn(0, n / T);
+    for (auto& th : pool)
+        th.join();
 }
 
 template <typename T>
@@ -487,23 +502,26 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
     }
     std::vector<int4> coo((size_t)total);
     std::vector<double> v64(c->dtype == BTC_DTYPE_F64 ? (size_t)total : 0);
-    for (size_t b = 0; b < s.blocks.size(); b++) {
-        if (boff[b] < 0)
-            continue;
-        long long o = boff[b];
-        for (int32_t e : s.blocks[b].ent) {
-            float fv = (float)tval[e];
-            int4 q;
-            q.x = txyz[3 * (int64_t)e];
-            q.y = txyz[3 * (int64_t)e + 1];
-            q.z = txyz[3 * (int64_t)e + 2];
-            std::memcpy(&q.w, &fv, 4);
-            coo[(size_t)o] = q;
-            if (!v64.empty())
-                v64[(size_t)o] = tval[e];
-            o++;
+    const int HT = default_threads(cfg);
+    parallel_for((int64_t)s.blocks.size(), HT, [&](int64_t b0, int64_t b1) {
+        for (int64_t b = b0; b < b1; b++) {
+            if (boff[(size_t)b] < 0)
+                continue;
+            long long o = boff[(size_t)b];
+            for (int32_t e : s.blocks[(size_t)b].ent) {
+                float fv = (float)tval[e];
+                int4 q;
+                q.x = txyz[3 * (int64_t)e];
+                q.y = txyz[3 * (int64_t)e + 1];
+                q.z = txyz[3 * (int64_t)e + 2];
+                std::memcpy(&q.w, &fv, 4);
+                coo[(size_t)o] = q;
+                if (!v64.empty())
+                    v64[(size_t)o] = tval[e];
+                o++;
+            }
         }
-    }
+    }, 256);
     std::vector<long long> soff(nslots);
     std::vector<int> snnz(nslots);
     std::vector<double> coe64(3 * (size_t)nslots);
@@ -548,8 +566,10 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
     int64_t en[2] = {ntr, nte};
     for (int k = 0; k < 2; k++) {
         std::vector<int4> q((size_t)en[k]);
-        for (int64_t i = 0; i < en[k]; i++)
-            q[(size_t)i] = make_int4(exyz[k][3 * i], exyz[k][3 * i + 1], exyz[k][3 * i + 2], 0);
+        parallel_for(en[k], HT, [&](int64_t lo, int64_t hi) {
+            for (int64_t i = lo; i < hi; i++)
+                q[(size_t)i] = make_int4(exyz[k][3 * i], exyz[k][3 * i + 1], exyz[k][3 * i + 2], 0);
+        });
         if ((rc = upload((void**)&c->eval_coo[k], q.data(), q.size() * sizeof(int4), c->stream)))
             return rc;
         if ((rc = upload((void**)&c->eval_val[k], eval[k], (size_t)en[k] * 8, c->stream)))
@@ -601,24 +621,26 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
             c->blk_ntiles[i] = ts.block_ntiles[(size_t)c->blk_ids[i]];
         }
         c->tile_feat.assign(ts.tiles.size() * BTC_TILE_FEATURES, 0.f);
-        for (size_t t = 0; t < ts.tiles.size(); t++) {
-            const btc::TileHdr& h = ts.tiles[t];
-            int maxseg = 0;
-            for (int q = 0; q < h.nseg; q++)
-                maxseg = std::max(maxseg, ts.segs[(size_t)(h.soff + q)].w);
-            float* f = &c->tile_feat[t * BTC_TILE_FEATURES];
-            const float nr = (float)std::max(1, h.nrows);
-            f[0] = (float)h.n / (float)c->st_wave;
-            f[1] = (float)h.nrows / (float)c->st_cap;
-            f[2] = (float)h.nx / nr;
-            f[3] = (float)h.ny / nr;
-            f[4] = (float)h.nseg / (float)std::max(1, h.n);
-            f[5] = (float)maxseg / 16.f;
-            f[6] = std::log2(1.f + (float)h.n) / 10.f;
-            f[7] = std::log2(1.f + (float)h.nrows) / 10.f;
-            f[8] = (float)h.n / nr / 8.f;
-            f[9] = 0.f;
-        }
+        parallel_for((int64_t)ts.tiles.size(), HT, [&](int64_t t0_, int64_t t1_) {
+            for (int64_t t = t0_; t < t1_; t++) {
+                const btc::TileHdr& h = ts.tiles[(size_t)t];
+                int maxseg = 0;
+                for (int q = 0; q < h.nseg; q++)
+                    maxseg = std::max(maxseg, ts.segs[(size_t)(h.soff + q)].w);
+                float* f = &c->tile_feat[(size_t)t * BTC_TILE_FEATURES];
+                const float nr = (float)std::max(1, h.nrows);
+                f[0] = (float)h.n / (float)c->st_wave;
+                f[1] = (float)h.nrows / (float)c->st_cap;
+                f[2] = (float)h.nx / nr;
+                f[3] = (float)h.ny / nr;
+                f[4] = (float)h.nseg / (float)std::max(1, h.n);
+                f[5] = (float)maxseg / 16.f;
+                f[6] = std::log2(1.f + (float)h.n) / 10.f;
+                f[7] = std::log2(1.f + (float)h.nrows) / 10.f;
+                f[8] = (float)h.n / nr / 8.f;
+                f[9] = 0.f;
+            }
+        }, 4096);
         for (size_t b = 0; b < ts.block_tile0.size(); b++)
             if (ts.block_tile0[b] >= 0)
                 c->tile_feat[(size_t)ts.block_tile0[b] * BTC_TILE_FEATURES + 9] = 1.f;
@@ -638,14 +660,21 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
             // (4; segments hold <= 16 entries), start in the mode's CSR list
             // (12; a tile holds <= 4096 entries)
             std::vector<uint32_t> seg32(ts.segs.size());
-            for (size_t q = 0; q < ts.segs.size(); q++) {
-                const int4& g = ts.segs[q];
-                if (g.x < 0 || g.x >= (1 << 14) || g.y < 0 || g.y > 2 || g.w < 1 || g.w > 16 || g.z < 0 ||
-                    g.z >= (1 << 12))
-                    return BTC_ERR_UNSUPPORTED;
-                seg32[q] = (uint32_t)g.x | ((uint32_t)g.y << 14) | ((uint32_t)(g.w - 1) << 16) |
-                           ((uint32_t)g.z << 20);
-            }
+            std::atomic<bool> bad_seg(false);
+            parallel_for((int64_t)ts.segs.size(), HT, [&](int64_t lo, int64_t hi) {
+                for (int64_t q = lo; q < hi; q++) {
+                    const int4& g = ts.segs[(size_t)q];
+                    if (g.x < 0 || g.x >= (1 << 14) || g.y < 0 || g.y > 2 || g.w < 1 || g.w > 16 || g.z < 0 ||
+                        g.z >= (1 << 12)) {
+                        bad_seg = true;
+                        return;
+                    }
+                    seg32[(size_t)q] = (uint32_t)g.x | ((uint32_t)g.y << 14) | ((uint32_t)(g.w - 1) << 16) |
+                                       ((uint32_t)g.z << 20);
+                }
+            });
+            if (bad_seg)
+                return BTC_ERR_UNSUPPORTED;
             if ((rc = upload((void**)&c->tsegs, seg32.data(), seg32.size() * 4, c->stream)))
                 return rc;
         }
@@ -662,21 +691,69 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
         std::vector<int64_t> cnts[3];
         std::vector<char> fast[3];
         {
+            // counted in a fixed number of slot ranges (partial sums added in
+            // range order), so the result does not depend on the thread count
             std::vector<double> decay[3];
             for (int a = 0; a < 3; a++) {
                 cnts[a].assign((size_t)c->rows[a], 0);
                 decay[a].assign((size_t)c->rows[a], 0.0);
             }
-            for (int k = 0; k < nslots; k++) {
-                double d[3];
-                for (int a = 0; a < 3; a++)
-                    d[a] = s.slot_coe[3 * (size_t)k + a] * cfg.lr * cfg.reg;
-                for (int32_t e : s.blocks[(size_t)s.slot_block[k]].ent)
+            const int P = c->updates >= (1LL << 24) ? 16 : 1;
+            std::vector<std::vector<int64_t>> pc((size_t)P - 1);
+            std::vector<std::vector<double>> pd((size_t)P - 1);
+            auto count_range = [&](int part) {
+                int64_t* cn[3];
+                double* dc[3];
+                const size_t off[3] = {0, (size_t)c->rows[0], (size_t)(c->rows[0] + c->rows[1])};
+                if (part == 0) {
                     for (int a = 0; a < 3; a++) {
-                        const size_t r = (size_t)txyz[3 * (int64_t)e + a];
-                        cnts[a][r]++;
-                        decay[a][r] += d[a];
+                        cn[a] = cnts[a].data();
+                        dc[a] = decay[a].data();
                     }
+                } else {
+                    const size_t all = (size_t)(c->rows[0] + c->rows[1] + c->rows[2]);
+                    pc[(size_t)part - 1].assign(all, 0);
+                    pd[(size_t)part - 1].assign(all, 0.0);
+                    for (int a = 0; a < 3; a++) {
+                        cn[a] = pc[(size_t)part - 1].data() + off[a];
+                        dc[a] = pd[(size_t)part - 1].data() + off[a];
+                    }
+                }
+                for (int k = (int)((int64_t)nslots * part / P); k < (int)((int64_t)nslots * (part + 1) / P); k++) {
+                    double d[3];
+                    for (int a = 0; a < 3; a++)
+                        d[a] = s.slot_coe[3 * (size_t)k + a] * cfg.lr * cfg.reg;
+                    for (int32_t e : s.blocks[(size_t)s.slot_block[k]].ent)
+                        for (int a = 0; a < 3; a++) {
+                            const size_t r = (size_t)txyz[3 * (int64_t)e + a];
+                            cn[a][r]++;
+                            dc[a][r] += d[a];
+                        }
+                }
+            };
+            {
+                std::atomic<int> nextp(0);
+                const int nt = std::max(1, std::min(HT, P));
+                std::vector<std::thread> pool;
+                auto worker = [&]() {
+                    for (int q; (q = nextp.fetch_add(1)) < P;)
+                        count_range(q);
+                };
+                for (int t = 1; t < nt; t++)
+                    pool.emplace_back(worker);
+                worker();
+                for (auto& th : pool)
+                    th.join();
+            }
+            for (int a = 0; a < 3; a++) {
+                const size_t off = a == 0 ? 0 : (a == 1 ? (size_t)c->rows[0] : (size_t)(c->rows[0] + c->rows[1]));
+                parallel_for(c->rows[a], HT, [&](int64_t lo, int64_t hi) {
+                    for (int q = 0; q + 1 < P; q++)
+                        for (int64_t r = lo; r < hi; r++) {
+                            cnts[a][(size_t)r] += pc[(size_t)q][off + (size_t)r];
+                            decay[a][(size_t)r] += pd[(size_t)q][off + (size_t)r];
+                        }
+                });
             }
             const double share = (double)c->sms * 8.0 / (double)std::max<size_t>(1, ts.tiles.size());
             for (int a = 0; a < 3; a++) {
@@ -707,13 +784,34 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
                 std::vector<char> is_hot((size_t)c->rows[a], 0);
                 for (int64_t r = 0; r < c->rows[a]; r++)
                     is_hot[(size_t)r] = cnt[(size_t)r] > 0 && (double)cnt[(size_t)r] >= thr;
-                for (const btc::TileHdr& h : ts.tiles)
-                    for (int q = 1; q < h.nseg; q++) {
-                        const int4& s0 = ts.segs[(size_t)(h.soff + q - 1)];
-                        const int4& s1 = ts.segs[(size_t)(h.soff + q)];
-                        if (s1.y == a && s0.y == a && s0.x == s1.x)
-                            is_hot[(size_t)ts.rows[(size_t)(h.roff + s1.x)]] = 1;
-                    }
+                {
+                    // rows a tile updates through more than one segment; each
+                    // thread collects its tiles' rows, then they are marked
+                    const int nt = ts.tiles.size() >= 4096 ? std::max(1, std::min(HT, 64)) : 1;
+                    std::vector<std::vector<int32_t>> multi((size_t)nt);
+                    std::vector<std::thread> pool;
+                    auto scan = [&](int t) {
+                        const size_t lo = ts.tiles.size() * (size_t)t / (size_t)nt;
+                        const size_t hi = ts.tiles.size() * (size_t)(t + 1) / (size_t)nt;
+                        for (size_t i = lo; i < hi; i++) {
+                            const btc::TileHdr& h = ts.tiles[i];
+                            for (int q = 1; q < h.nseg; q++) {
+                                const int4& s0 = ts.segs[(size_t)(h.soff + q - 1)];
+                                const int4& s1 = ts.segs[(size_t)(h.soff + q)];
+                                if (s1.y == a && s0.y == a && s0.x == s1.x)
+                                    multi[(size_t)t].push_back(ts.rows[(size_t)(h.roff + s1.x)]);
+                            }
+                        }
+                    };
+                    for (int t = 1; t < nt; t++)
+                        pool.emplace_back(scan, t);
+                    scan(0);
+                    for (auto& th : pool)
+                        th.join();
+                    for (const auto& v : multi)
+                        for (int32_t r : v)
+                            is_hot[(size_t)r] = 1;
+                }
                 std::vector<int> hot;
                 for (int64_t r = 0; r < c->rows[a]; r++)
                     if (is_hot[(size_t)r] || fast[a][(size_t)r])  // FAST rows decay from their master
@@ -734,23 +832,31 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
             // the kernel finds a row's master in its staged row id: ~(master
             // index, FAST bit for a FAST row) instead of the global row, so
             // staging needs no lookup
-            for (const btc::TileHdr& h : ts.tiles)
-                for (int r = 0; r < h.nrows; r++) {
-                    const int m = r < h.nx ? 0 : (r < h.nx + h.ny ? 1 : 2);
-                    int32_t& g = ts.rows[(size_t)(h.roff + r)];
-                    const int hm = maps[m][(size_t)g];
-                    if (hm >= 0)
-                        g = ~(hm | (fast[m][(size_t)g] ? FAST : 0));
+            parallel_for((int64_t)ts.tiles.size(), HT, [&](int64_t lo, int64_t hi) {
+                for (int64_t i = lo; i < hi; i++) {
+                    const btc::TileHdr& h = ts.tiles[(size_t)i];
+                    for (int r = 0; r < h.nrows; r++) {
+                        const int m = r < h.nx ? 0 : (r < h.nx + h.ny ? 1 : 2);
+                        int32_t& g = ts.rows[(size_t)(h.roff + r)];
+                        const int hm = maps[m][(size_t)g];
+                        if (hm >= 0)
+                            g = ~(hm | (fast[m][(size_t)g] ? FAST : 0));
+                    }
                 }
+            }, 4096);
         } else {
             // FP32/FP64: a FAST row's staged id is ~row
-            for (const btc::TileHdr& h : ts.tiles)
-                for (int r = 0; r < h.nrows; r++) {
-                    const int m = r < h.nx ? 0 : (r < h.nx + h.ny ? 1 : 2);
-                    int32_t& g = ts.rows[(size_t)(h.roff + r)];
-                    if (fast[m][(size_t)g])
-                        g = ~g;
+            parallel_for((int64_t)ts.tiles.size(), HT, [&](int64_t lo, int64_t hi) {
+                for (int64_t i = lo; i < hi; i++) {
+                    const btc::TileHdr& h = ts.tiles[(size_t)i];
+                    for (int r = 0; r < h.nrows; r++) {
+                        const int m = r < h.nx ? 0 : (r < h.nx + h.ny ? 1 : 2);
+                        int32_t& g = ts.rows[(size_t)(h.roff + r)];
+                        if (fast[m][(size_t)g])
+                            g = ~g;
+                    }
                 }
+            }, 4096);
         }
         if ((rc = upload((void**)&c->trows, ts.rows.data(), ts.rows.size() * 4, c->stream)))
             return rc;

@@ -313,3 +313,47 @@ def test_cli_arguments_like_the_reference():
     r = subprocess.run([cli, "ds", "10", "10", "10", "/tmp", "0", "/tmp", "--rank", "101", "--bin-cache", "/tmp",
                         "--precision", "bf16", "--mode", "staged"], capture_output=True, text=True)
     assert r.returncode == 1 and "Unknown option" not in r.stderr and "rank r must be in [1, 100]" in r.stderr
+
+
+@pytest.mark.parametrize("dims,nnz,zipf,block_s", [((20000, 20000, 5000), 300_000, (1.2, 1.2, 1.2), 256),
+                                                   ((50000, 500, 200000), 400_000, (1.5, 0.0, 1.5), 1024),
+                                                   ((300, 200, 100), 50_000, (0.0, 0.0, 0.0), 64)])
+def test_learned_blocking_schedules_every_entry_once_in_conflict_free_groups(dims, nnz, zipf, block_s):
+    """The learned blocking (no model: split axes in turn) is a partition of
+    the train entries into boxes of at most block_s entries, each block once
+    per epoch (no padding), grouped so that no two blocks of a group share a
+    row of any mode; every coe weight is 1."""
+    I, J, K = dims
+    tx, _, _, _ = bg.gen_tensor(I, J, K, nnz, zipf=zipf, gt_rank=2, train_frac=1.0, seed=11)
+    tx, _ = bg.shuffle(tx, np.zeros(len(tx)))
+    cfg = bg.config(I=I, J=J, K=K, block_s=block_s, parallel_sequence_size=8, resident_blocks=-1)
+    s = bg.Schedule(cfg, tx, learned=True)
+    sm = s.summary
+    assert sm.scheduled_updates == len(tx) and sm.num_slots == sm.num_blocks
+    boxes = s.boxes()
+    seen = np.zeros(len(tx), np.int64)
+    for b in range(sm.num_blocks):
+        e = s.block_entries(b)
+        assert 0 < len(e) <= block_s
+        assert np.all(np.diff(e) > 0)  # input order kept inside a block
+        seen[e] += 1
+        c = tx[e]
+        assert (c >= boxes[b, :, 0]).all() and (c < boxes[b, :, 1]).all()
+    assert (seen == 1).all()
+    off, ids, coe = s.groups()
+    assert np.all(coe == 1.0) and sorted(ids.tolist()) == list(range(sm.num_blocks))
+    for g in range(len(off) - 1):
+        bl = ids[off[g]:off[g + 1]]
+        assert 1 <= len(bl) <= 8
+        lo, hi = boxes[bl, :, 0], boxes[bl, :, 1]
+        overlap = (lo[:, None, :] < hi[None, :, :]) & (lo[None, :, :] < hi[:, None, :])
+        np.fill_diagonal(overlap[:, :, 0], False)
+        np.fill_diagonal(overlap[:, :, 1], False)
+        np.fill_diagonal(overlap[:, :, 2], False)
+        assert not overlap.any()
+    # deterministic for any thread count
+    s1 = bg.Schedule(bg.config(I=I, J=J, K=K, block_s=block_s, parallel_sequence_size=8, resident_blocks=-1,
+                               host_threads=1), tx, learned=True)
+    assert np.array_equal(s1.boxes(), boxes)
+    for x, y in zip(s1.groups(), s.groups()):
+        assert np.array_equal(x, y)
