@@ -603,6 +603,7 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
             return BTC_ERR_UNSUPPORTED;  // one entry needs three staged rows
         btc::TileSet ts;
         btc::build_tiles(s, txyz, tval, cfg.I, cfg.J, cfg.K, c->st_cap, c->st_wave, 16,
+                         cfg.row_repeat > 0 ? cfg.row_repeat : 16,
                          c->dtype == BTC_DTYPE_F64, ts, default_threads(cfg));
         std::vector<int> t0(nslots), tn(nslots);
         for (int k = 0; k < nslots; k++) {

@@ -2,8 +2,14 @@
 //
 // A scheduled block's entries are taken in block order and cut into tiles
 // when the tile reaches `wave` entries (the reference kernel's concurrency
-// unit: one pass of thread_size threads over a slot, sgd_Kernel.cu:358-392)
-// or when one more entry would need more than `cap` distinct rows.  For each
+// unit: one pass of thread_size threads over a slot, sgd_Kernel.cu:358-392),
+// when one more entry would need more than `cap` distinct rows, or when it
+// would put a row into the tile for the (repeat + 1)-th time.  Every entry of
+// a tile reads the rows as they were when the tile started, so a row met c
+// times in one tile takes c updates computed from one snapshot: a Jacobi
+// step whose gain grows as lr * c * |other rows|^2, which diverged on skewed
+// tensors (hot rows met hundreds of times per tile) once the factors had
+// grown; the repeat bound keeps c small.  For each
 // mode the tile's entries are counting-sorted by row (CSR) and every row's
 // list is split into owner segments of at most `seg` entries; a segment is
 // the unit one lane group reduces before a single shared-memory add.
@@ -20,7 +26,7 @@ namespace {
 // to `out`); first[i] / count[i] receive block blk[i]'s first tile and tile
 // count.
 void build_range(const Schedule& s, const int32_t* xyz, const double* val, const int* dims, int cap, int wave,
-                 int seg, bool want64, const int* blk, size_t nb, TileSet& out, int* first, int* count)
+                 int seg, int repeat, bool want64, const int* blk, size_t nb, TileSet& out, int* first, int* count)
 {
     std::vector<int> stamp[3], loc[3];
     for (int a = 0; a < 3; a++) {
@@ -29,6 +35,7 @@ void build_range(const Schedule& s, const int32_t* xyz, const double* val, const
     }
     int tile_id = 0;
     std::vector<int32_t> rows_m[3];
+    std::vector<int32_t> uses_m[3];  // entries of the current tile per staged row
     struct Ent {
         int32_t e;
         uint16_t l[3];
@@ -93,8 +100,10 @@ void build_range(const Schedule& s, const int32_t* xyz, const double* val, const
         out.max_n = std::max(out.max_n, h.n);
         out.tiles.push_back(h);
         cur.clear();
-        for (int a = 0; a < 3; a++)
+        for (int a = 0; a < 3; a++) {
             rows_m[a].clear();
+            uses_m[a].clear();
+        }
         tile_id++;
     };
 
@@ -104,10 +113,14 @@ void build_range(const Schedule& s, const int32_t* xyz, const double* val, const
         for (int32_t e : s.blocks[(size_t)b].ent) {
             const int32_t* c = xyz + 3 * (int64_t)e;
             int need = 0;
-            for (int a = 0; a < 3; a++)
-                need += stamp[a][(size_t)c[a]] != tile_id;
+            bool full_row = false;
+            for (int a = 0; a < 3; a++) {
+                const bool in = stamp[a][(size_t)c[a]] == tile_id;
+                need += !in;
+                full_row |= in && uses_m[a][(size_t)loc[a][(size_t)c[a]]] >= repeat;
+            }
             int nrows = (int)(rows_m[0].size() + rows_m[1].size() + rows_m[2].size());
-            if (!cur.empty() && ((int)cur.size() >= wave || nrows + need > cap)) {
+            if (!cur.empty() && ((int)cur.size() >= wave || nrows + need > cap || full_row)) {
                 close();
             }
             Ent q;
@@ -117,8 +130,10 @@ void build_range(const Schedule& s, const int32_t* xyz, const double* val, const
                     stamp[a][(size_t)c[a]] = tile_id;
                     loc[a][(size_t)c[a]] = (int)rows_m[a].size();
                     rows_m[a].push_back(c[a]);
+                    uses_m[a].push_back(0);
                 }
                 q.l[a] = (uint16_t)loc[a][(size_t)c[a]];
+                uses_m[a][(size_t)q.l[a]]++;
             }
             cur.push_back(q);
         }
@@ -135,7 +150,7 @@ void build_range(const Schedule& s, const int32_t* xyz, const double* val, const
 // are concatenated in order with their offsets moved: the result does not
 // depend on the thread count.
 void build_tiles(const Schedule& s, const int32_t* xyz, const double* val, int I, int J, int K, int cap,
-                 int wave, int seg, bool want64, TileSet& out, int threads)
+                 int wave, int seg, int repeat, bool want64, TileSet& out, int threads)
 {
     out = TileSet();
     const int dims[3] = {I, J, K};
@@ -167,7 +182,8 @@ void build_tiles(const Schedule& s, const int32_t* xyz, const double* val, int I
     std::vector<int> first(order.size()), count(order.size());
     auto work = [&](int t) {
         const size_t lo = cut[(size_t)t], hi = cut[(size_t)t + 1];
-        build_range(s, xyz, val, dims, cap, wave, seg, want64, order.data() + lo, hi - lo, part[(size_t)t],
+        build_range(s, xyz, val, dims, cap, wave, seg, std::max(1, repeat), want64, order.data() + lo, hi - lo,
+                    part[(size_t)t],
                     first.data() + lo, count.data() + lo);
     };
     std::vector<std::thread> pool;

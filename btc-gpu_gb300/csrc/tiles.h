@@ -38,9 +38,10 @@ struct TileSet {
 };
 
 // cap: rows per tile; wave: entries per tile; seg: entries per owner segment;
-// want64: also keep FP64 entry values; threads: host threads to use (the
-// result does not depend on it).
+// repeat: most entries of any one row in a tile; want64: also keep FP64
+// entry values; threads: host threads to use (the result does not depend on
+// it).
 void build_tiles(const Schedule& s, const int32_t* xyz, const double* val, int I, int J, int K, int cap,
-                 int wave, int seg, bool want64, TileSet& out, int threads = 1);
+                 int wave, int seg, int repeat, bool want64, TileSet& out, int threads = 1);
 
 }  // namespace btc

@@ -38,7 +38,7 @@ class Config(ctypes.Structure):
         ("dtype", ctypes.c_int32), ("mode", ctypes.c_int32), ("device", ctypes.c_int32),
         ("resident_blocks", ctypes.c_int32), ("chunk", ctypes.c_int32),
         ("host_threads", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 6),
+        ("row_repeat", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5),
     ]
 
 

@@ -89,7 +89,8 @@ typedef struct btc_config {
     int32_t chunk;                  /* entries per Hogwild work item, 0 = auto */
     int32_t host_threads;           /* builder threads, 0 = hardware concurrency */
     int32_t ctas_per_sm;            /* staged kernel: CTAs sharing one SM's shared memory, 0 = auto */
-    int32_t reserved[6];
+    int32_t row_repeat;             /* staged kernel: most entries of one row in a tile, 0 = 16 */
+    int32_t reserved[5];
 } btc_config;
 
 typedef struct btc_schedule_summary {

@@ -33,14 +33,15 @@ def agreement(F, R, F0):
 
 
 def bf16_ulp_residual(F, R):
-    """RMS of (F - R) in units of one BF16 ulp of R (8 significant bits),
-    over every element of every mode."""
+    """RMS of (F - R) over every element, in units of one BF16 ulp (8
+    significant bits) of each mode's RMS value (elements near zero have
+    far smaller ulps than the rows' typical ones, so a per-element ulp would
+    let them dominate)."""
     tot, cnt = 0.0, 0
     for f, r in zip(F, R):
-        a = np.maximum(np.abs(r), 2.0 ** -30)
-        _, e = np.frexp(a)  # a = m 2^e, m in [0.5, 1): ulp = 2^(e - 8)
-        ulp = np.ldexp(1.0, e - 8)
-        q = (f - r) / ulp
+        rms = max(float(np.sqrt((r * r).mean())), 2.0 ** -30)
+        _, e = np.frexp(rms)  # rms = m 2^e, m in [0.5, 1): ulp = 2^(e - 8)
+        q = (f - r) / np.ldexp(1.0, e - 8)
         tot += float((q * q).sum())
         cnt += q.size
     return float(np.sqrt(tot / max(cnt, 1)))
