@@ -244,7 +244,7 @@ btc_status btc_config_validate(const btc_config* c)
     if (c->thread_size <= 0 || c->thread_size > 1024 || c->parallel_sequence_size < 0 ||
         c->requested_gpu_count < 0)
         return BTC_ERR_ARG;
-    if (c->dtype < 0 || c->dtype > 2 || c->mode < 0 || c->mode > 2 || c->chunk < 0)
+    if (c->dtype < 0 || c->dtype > 2 || c->mode < 0 || c->mode > 3 || c->chunk < 0)
         return BTC_ERR_ARG;
     return BTC_OK;
 }
@@ -468,6 +468,20 @@ static btc_status upload(void** dst, const void* src, size_t bytes, cudaStream_t
 static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* txyz, const double* tval,
                             int64_t ntr, const int32_t* sxyz, const double* sval, int64_t nte)
 {
+    // the slots the context runs: the balanced groups' slots, or for the
+    // lock-free mode every non-empty block once in strata order with coe 1
+    // (ToMatrix_LF, block.cu:1192-1217)
+    std::vector<int32_t> lf_slots;
+    std::vector<double> lf_coe;
+    if (c->cfg.mode == BTC_MODE_LOCKFREE) {
+        for (int32_t b : s.strata_ids)
+            if (!s.blocks[(size_t)b].ent.empty())
+                lf_slots.push_back(b);
+        lf_coe.assign(3 * lf_slots.size(), 1.0);
+    }
+    const bool lf = c->cfg.mode == BTC_MODE_LOCKFREE;
+    const std::vector<int32_t>& slot_block = lf ? lf_slots : slot_block;
+    const std::vector<double>& slot_coe = lf ? lf_coe : slot_coe;
     const btc_config& cfg = c->cfg;
     CK(cudaSetDevice(cfg.device));
     cudaDeviceProp prop;
@@ -480,6 +494,8 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
     c->mode = cfg.mode;
     if (c->dtype == BTC_DTYPE_BF16 && c->mode != BTC_MODE_STAGED)
         return BTC_ERR_UNSUPPORTED;  // BF16 storage is served by the staged kernel
+    if (c->mode == BTC_MODE_LOCKFREE && s.learned)
+        return BTC_ERR_UNSUPPORTED;  // the lock-free rule runs on the reference's strata
     c->esize = c->dtype == BTC_DTYPE_F64 ? 8 : (c->dtype == BTC_DTYPE_BF16 ? 2 : 4);
     c->R = cfg.rank;
     c->Rp = btc::padded_rank(c->dtype, c->R);
@@ -489,12 +505,12 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
     c->rows[2] = cfg.K;
 
     // entry stream: each scheduled block once, in order of first use
-    const int nslots = (int)s.slot_block.size();
+    const int nslots = (int)slot_block.size();
     c->nslots = nslots;
     std::vector<long long> boff(s.blocks.size(), -1);
     long long total = 0;
     for (int k = 0; k < nslots; k++) {
-        int b = s.slot_block[k];
+        int b = slot_block[k];
         if (boff[b] < 0) {
             boff[b] = total;
             total += (long long)s.blocks[b].ent.size();
@@ -529,19 +545,19 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
     std::vector<int2> items;
     c->updates = 0;
     for (int k = 0; k < nslots; k++) {
-        int b = s.slot_block[k];
+        int b = slot_block[k];
         soff[k] = boff[b];
         snnz[k] = (int)s.blocks[b].ent.size();
         c->updates += snnz[k];
         for (int a = 0; a < 3; a++) {
-            coe64[3 * k + a] = s.slot_coe[3 * k + a] * cfg.lr;  // (coe*lr) as the reference groups it
+            coe64[3 * k + a] = slot_coe[3 * k + a] * cfg.lr;  // (coe*lr) as the reference groups it
             coe32[3 * k + a] = (float)coe64[3 * k + a];
         }
         for (int st = 0; st < snnz[k]; st += c->chunk)
             items.push_back(make_int2(k, st));
     }
     c->nitems = (long long)items.size();
-    c->coe_host.assign(s.slot_coe.begin(), s.slot_coe.end());
+    c->coe_host.assign(slot_coe.begin(), slot_coe.end());
     btc_status rc;
     if ((rc = upload((void**)&c->coo, coo.data(), coo.size() * sizeof(int4), c->stream)))
         return rc;
@@ -607,8 +623,8 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
                          c->dtype == BTC_DTYPE_F64, ts, default_threads(cfg));
         std::vector<int> t0(nslots), tn(nslots);
         for (int k = 0; k < nslots; k++) {
-            t0[k] = ts.block_tile0[(size_t)s.slot_block[k]];
-            tn[k] = ts.block_ntiles[(size_t)s.slot_block[k]];
+            t0[k] = ts.block_tile0[(size_t)slot_block[k]];
+            tn[k] = ts.block_ntiles[(size_t)slot_block[k]];
         }
         c->st_tiles = (long long)ts.tiles.size();
         c->st_rows = (long long)ts.rows.size();
@@ -723,8 +739,8 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
                 for (int k = (int)((int64_t)nslots * part / P); k < (int)((int64_t)nslots * (part + 1) / P); k++) {
                     double d[3];
                     for (int a = 0; a < 3; a++)
-                        d[a] = s.slot_coe[3 * (size_t)k + a] * cfg.lr * cfg.reg;
-                    for (int32_t e : s.blocks[(size_t)s.slot_block[k]].ent)
+                        d[a] = slot_coe[3 * (size_t)k + a] * cfg.lr * cfg.reg;
+                    for (int32_t e : s.blocks[(size_t)slot_block[k]].ent)
                         for (int a = 0; a < 3; a++) {
                             const size_t r = (size_t)txyz[3 * (int64_t)e + a];
                             cn[a][r]++;
@@ -879,7 +895,7 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
         CK(cudaStreamSynchronize(c->stream));  // host tile arrays go out of scope
     }
 
-    if (c->mode == BTC_MODE_DETERMINISTIC) {
+    if (c->mode == BTC_MODE_DETERMINISTIC || c->mode == BTC_MODE_LOCKFREE) {
         // slots that share any factor row run in schedule order; the others
         // run together (wave = 1 + latest wave of any row the slot touches)
         std::vector<int> last[3];
@@ -888,7 +904,7 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
         std::vector<int> wave(nslots);
         int nw = 0;
         for (int k = 0; k < nslots; k++) {
-            const auto& ent = s.blocks[s.slot_block[k]].ent;
+            const auto& ent = s.blocks[slot_block[k]].ent;
             int w = 0;
             for (int32_t e : ent)
                 for (int a = 0; a < 3; a++)
@@ -1088,10 +1104,13 @@ static btc_status enqueue_epoch(btc_ctx* c, int* launches)
     if (c->mode == BTC_MODE_HOGWILD) {
         CK(btc::launch_hogwild(c->dtype, a, c->hw_grid, c->hw_block, c->stream));
         n = c->nitems > 0 ? 1 : 0;
-    } else if (c->mode == BTC_MODE_DETERMINISTIC) {
+    } else if (c->mode == BTC_MODE_DETERMINISTIC || c->mode == BTC_MODE_LOCKFREE) {
         for (size_t w = 1; w + 1 < c->wave_off.size(); w++) {
             int b = c->wave_off[w], e = c->wave_off[w + 1];
-            CK(btc::launch_det_wave(c->dtype, c->wave_slots + b, e - b, a, c->stream));
+            if (c->mode == BTC_MODE_LOCKFREE)
+                CK(btc::launch_lf_wave(c->dtype, c->wave_slots + b, e - b, a, c->stream));
+            else
+                CK(btc::launch_det_wave(c->dtype, c->wave_slots + b, e - b, a, c->stream));
             n += e > b ? 1 : 0;
         }
     } else if (c->mode == BTC_MODE_STAGED) {

@@ -243,6 +243,59 @@ __global__ void __launch_bounds__(128) k_det(const int* wave_slots, int n, SgdAr
     }
 }
 
+// The lock-free rule (sgd_Kernel.cu:401-451) on one warp per block: entries
+// in block order; per element the A row moves first, B from the new A, C
+// from the new A and B.  Products are rounded as written: dot as
+// fma(a * b, c, dot), each update x + lr * ((e * u) * v - reg * x).
+template <typename T>
+__global__ void __launch_bounds__(128) k_lf(const int* wave_slots, int n, SgdArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31;
+    const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (w >= n)
+        return;  // the whole warp leaves together
+    T* sa = reinterpret_cast<T*>(smem_raw) + (size_t)(threadIdx.x >> 5) * 3 * a.Rp;
+    T* sb = sa + a.Rp;
+    T* sc = sb + a.Rp;
+    const int s = wave_slots[w];
+    const long long off = a.slot_off[s];
+    const int nnz = a.slot_nnz[s];
+    const T lr = static_cast<const T*>(a.slot_coe)[3 * s];  // coe 1 times lr
+    const T reg = (T)a.reg;
+    T* A = static_cast<T*>(a.A);
+    T* B = static_cast<T*>(a.B);
+    T* C = static_cast<T*>(a.C);
+    const int R = a.R, Rp = a.Rp;
+    for (int t = 0; t < nnz; t++) {
+        const int4 e = __ldg(&a.coo[off + t]);
+        const T v = entry_value<T>(e, a.val64, off + t);
+        T* pa = A + (size_t)e.x * Rp;
+        T* pb = B + (size_t)e.y * Rp;
+        T* pc = C + (size_t)e.z * Rp;
+        for (int q = lane; q < R; q += 32) {
+            sa[q] = __ldcg(pa + q);
+            sb[q] = __ldcg(pb + q);
+            sc[q] = __ldcg(pc + q);
+        }
+        __syncwarp();
+        T dot = T(0);
+        for (int q = 0; q < R; q++)
+            dot = fma_rn(mul_rn(sa[q], sb[q]), sc[q], dot);
+        const T err = sub_rn(v, dot);
+        for (int q = lane; q < R; q += 32) {
+            const T av = sa[q], bv = sb[q], cv = sc[q];
+            const T na = add_rn(av, mul_rn(lr, sub_rn(mul_rn(mul_rn(err, bv), cv), mul_rn(reg, av))));
+            const T nb = add_rn(bv, mul_rn(lr, sub_rn(mul_rn(mul_rn(err, na), cv), mul_rn(reg, bv))));
+            const T nc = add_rn(cv, mul_rn(lr, sub_rn(mul_rn(mul_rn(err, nb), na), mul_rn(reg, cv))));
+            __stcg(pa + q, na);
+            __stcg(pb + q, nb);
+            __stcg(pc + q, nc);
+        }
+        __syncwarp();
+    }
+}
+
 template <typename T, int G, int NV, typename ST = T>
 __global__ void __launch_bounds__(kMetricThreads) k_metrics(const int4* coo, const double* val,
                                                            long long n, const ST* A, const ST* B,
@@ -596,6 +649,24 @@ cudaError_t launch_det_wave(int dtype, const int* wave_slots, int n, const SgdAr
     } else if (dtype == 0) {
         size_t sm = (size_t)warps * 3 * a.Rp * sizeof(float);
         k_det<float><<<grid, warps * 32, sm, st>>>(wave_slots, n, a);
+    } else {
+        return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lf_wave(int dtype, const int* wave_slots, int n, const SgdArgs& a, cudaStream_t st)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    const int warps = 4;
+    const int grid = (n + warps - 1) / warps;
+    if (dtype == 1) {
+        size_t sm = (size_t)warps * 3 * a.Rp * sizeof(double);
+        k_lf<double><<<grid, warps * 32, sm, st>>>(wave_slots, n, a);
+    } else if (dtype == 0) {
+        size_t sm = (size_t)warps * 3 * a.Rp * sizeof(float);
+        k_lf<float><<<grid, warps * 32, sm, st>>>(wave_slots, n, a);
     } else {
         return cudaErrorInvalidValue;
     }

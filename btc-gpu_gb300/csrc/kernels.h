@@ -37,6 +37,8 @@ cudaError_t launch_hogwild(int dtype, const SgdArgs& a, int grid, int block, cud
 int hogwild_blocks_per_sm(int dtype, int R, int block);
 cudaError_t launch_det_wave(int dtype, const int* wave_slots, int n, const SgdArgs& a,
                             cudaStream_t st);
+// One wave of the lock-free rule (slot coe = lr, one block per slot).
+cudaError_t launch_lf_wave(int dtype, const int* wave_slots, int n, const SgdArgs& a, cudaStream_t st);
 // Metrics: FP64 sums of (ref - dot)^2, |ref - dot| and ref^2 over n entries;
 // per-CTA partials then a fixed-order sum into result[0..2].
 cudaError_t launch_metrics(int dtype, const int4* coo, const double* val, long long n,

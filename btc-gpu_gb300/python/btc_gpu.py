@@ -18,7 +18,7 @@ F32, F64, BF16 = 0, 1, 2
 NOALLOC_MAX_ENTRIES = 67108864
 BLOCK_FEATURES = 10
 TILE_FEATURES = 10
-HOGWILD, DETERMINISTIC, STAGED = 0, 1, 2
+HOGWILD, DETERMINISTIC, STAGED, LOCKFREE = 0, 1, 2, 3
 TRAIN, TEST = 0, 1
 
 

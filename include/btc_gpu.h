@@ -62,7 +62,16 @@ typedef enum btc_mode {
     BTC_MODE_DETERMINISTIC = 1,
     /* One CTA per slot: the slot's reused rows are staged in shared memory,
      * updated there, and each row is written back once as a delta. */
-    BTC_MODE_STAGED = 2
+    BTC_MODE_STAGED = 2,
+    /* The reference's lock-free variant (tensor_LF, sgd_Kernel.cu:401-451,
+     * ToMatrix_LF, block.cu:1192-1217): the conflict-free strata before
+     * padding, every block once, no coe weights, and the in-place rule
+     * a += lr(e b c - reg a), then b with the new a, then c with the new a
+     * and b, element by element.  Blocks run one warp each, entries in block
+     * order, blocks sharing a row in strata order (F32 / F64; the FP64
+     * instantiation equals the serial replay of the rule bit for bit).  The
+     * reference runs it on one CTA whose threads race on shared rows. */
+    BTC_MODE_LOCKFREE = 3
 } btc_mode;
 
 typedef enum btc_split { BTC_SPLIT_TRAIN = 0, BTC_SPLIT_TEST = 1 } btc_split;

@@ -21,6 +21,7 @@
  *   coe weights ................ block.cu:470-513 (union-find per axis)
  *   flattening ................. block.cu:1151-1190 (Preproccess_list)
  *   SGD update rule ............ sgd_Kernel.cu:336-351 (pre-update rows, coe*lr)
+ *   lock-free variant .......... sgd_Kernel.cu:401-451, block.cu:1192-1217
  *   test metrics ............... sgd_Kernel.cu:85-99, 188-199
  *
  * Build with -ffp-contract=off: the update rule is evaluated exactly as
@@ -688,6 +689,43 @@ int64_t orc_sgd_epoch(const orc_sched *s, const int32_t *xyz, const double *val,
         }
     }
     free(av);
+    return upd;
+}
+
+/* The lock-free variant (tensor_LF, sgd_Kernel.cu:401-451; its entry list
+ * ToMatrix_LF, block.cu:1192-1217): the conflict-free strata in order, every
+ * block of a stratum in order, every entry of a block in order, no coe
+ * weights.  The rows are updated in place element by element: A first, B
+ * from the new A, C from the new A and B.  Rounding as written in this
+ * restatement (the reference's own contraction is the compiler's choice):
+ * dot = fma(a * b, c, dot), x' = x + lr * ((e * u) * v - reg * x).  The
+ * reference reads one stratum count past the strata it fills (num_LF has
+ * num_parallel entries for num_parallel - 1 strata); only the filled strata
+ * are replayed here. */
+int64_t orc_lf_epoch(const orc_sched *s, const int32_t *xyz, const double *val, int R, double lr, double reg,
+                     double *A, double *B, double *C)
+{
+    int64_t upd = 0;
+    for (int i = 0; i < s->nstrata; i++)
+        for (int m = s->strata_off[i]; m < s->strata_off[i + 1]; m++) {
+            const orc_block *blk = &s->blocks[s->strata_ids[m]];
+            for (int t = 0; t < blk->nnz; t++) {
+                int e = blk->ent[t];
+                double *Ar = A + (size_t)xyz[3 * (int64_t)e] * R;
+                double *Br = B + (size_t)xyz[3 * (int64_t)e + 1] * R;
+                double *Cr = C + (size_t)xyz[3 * (int64_t)e + 2] * R;
+                double dot = 0.0;
+                for (int q = 0; q < R; q++)
+                    dot = fma(Ar[q] * Br[q], Cr[q], dot);
+                double err = val[e] - dot;
+                for (int q = 0; q < R; q++) {
+                    Ar[q] = Ar[q] + lr * ((err * Br[q]) * Cr[q] - reg * Ar[q]);
+                    Br[q] = Br[q] + lr * ((err * Ar[q]) * Cr[q] - reg * Br[q]);
+                    Cr[q] = Cr[q] + lr * ((err * Br[q]) * Ar[q] - reg * Cr[q]);
+                }
+                upd++;
+            }
+        }
     return upd;
 }
 

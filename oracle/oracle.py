@@ -45,6 +45,8 @@ def _load():
     lib.orc_groups.argtypes = [P, P, P, P]
     lib.orc_sgd_epoch.argtypes = [P, P, P, ctypes.c_int, ctypes.c_double, ctypes.c_double, P, P, P]
     lib.orc_sgd_epoch.restype = ctypes.c_int64
+    lib.orc_lf_epoch.argtypes = [P, P, P, ctypes.c_int, ctypes.c_double, ctypes.c_double, P, P, P]
+    lib.orc_lf_epoch.restype = ctypes.c_int64
     lib.orc_metrics.argtypes = [P, P, ctypes.c_int64, ctypes.c_int, P, P, P, P]
     lib.orc_sgd_replay.argtypes = [ctypes.c_int64, ctypes.c_int64, P, P, P, P, P, ctypes.c_int,
                                    ctypes.c_double, ctypes.c_double, P, P, P]
@@ -132,6 +134,14 @@ class Schedule:
             assert M.dtype == np.float64 and M.flags.c_contiguous
         return lib.orc_sgd_epoch(self._h, _ptr(self.xyz), _ptr(val), R, lr, reg, _ptr(A),
                                  _ptr(B), _ptr(C))
+
+    def lf_epoch(self, val, R, lr, reg, A, B, C):
+        """One serial FP64 epoch of the lock-free variant in place on A, B, C."""
+        lib = _load()
+        val = np.ascontiguousarray(val, dtype=np.float64)
+        for M in (A, B, C):
+            assert M.dtype == np.float64 and M.flags.c_contiguous
+        return lib.orc_lf_epoch(self._h, _ptr(self.xyz), _ptr(val), R, lr, reg, _ptr(A), _ptr(B), _ptr(C))
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -350,3 +350,47 @@ def test_bf16_staged_moves_factors_like_the_oracle(case_name, R):
     assert ok, why
     assert not check_bf16(start, ref, start)[0]
     assert not check_bf16(half, ref, start)[0]
+
+
+@pytest.mark.parametrize("case_name,R", [("uniform_3k", 16), ("zipf13_6k", 16), ("zipf_bs4_dup", 8), ("bigdim", 100)])
+def test_lockfree_f64_equals_the_serial_lockfree_rule(case_name, R):
+    """The lock-free variant (tensor_LF): every block of the conflict-free
+    strata once, in-place A-then-B-then-C updates without coe weights; FP64
+    epochs equal the oracle's serial replay of that rule bit for bit."""
+    c, xyz, val, init, sched = _setup(case_name, R)
+    ref = [m.copy() for m in init]
+    ctx = _ctx(c, xyz, val, R, bg.F64, bg.LOCKFREE)
+    for m in range(3):
+        ctx.set_factors(m, init[m])
+    for epoch in range(3):
+        upd = sched.lf_epoch(val, R, LR, REG, *ref)
+        st = ctx.train_epoch()
+        assert st.updates == upd == len(val) and st.device_status == 0
+        for m in range(3):
+            got = ctx.get_factors(m)
+            assert np.array_equal(got, ref[m]), (epoch, m, np.abs(got - ref[m]).max())
+
+
+@pytest.mark.parametrize("case_name,R", [("cube1000_20k", 16), ("zipf13_6k", 32)])
+def test_lockfree_f32_moves_factors_like_the_oracle(case_name, R):
+    c, xyz, val, init, sched = _setup(case_name, R)
+    ctx = _ctx(c, xyz, val, R, bg.F32, bg.LOCKFREE)
+    for m in range(3):
+        ctx.set_factors(m, init[m])
+    start = [ctx.get_factors(m) for m in range(3)]
+    ref = [m.copy() for m in start]
+    half = [m.copy() for m in start]
+    sched.lf_epoch(val, R, LR, REG, *ref)
+    sched.lf_epoch(val, R, LR / 2, REG, *half)
+    ctx.train_epoch()
+    got = [ctx.get_factors(m) for m in range(3)]
+    ok, why = check_fp(got, ref, start, dev_tol=1e-3, slope_tol=1e-3)
+    assert ok, why
+    assert not check_fp(half, ref, start)[0]
+
+
+def test_lockfree_has_no_bf16_form():
+    c, xyz, val, init, sched = _setup("uniform_3k", 8)
+    with pytest.raises(bg.BtcError) as e:
+        _ctx(c, xyz, val, 8, bg.BF16, bg.LOCKFREE)
+    assert e.value.status == 7  # BTC_ERR_UNSUPPORTED
