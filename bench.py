@@ -430,10 +430,16 @@ def run_gpu(args):
         return c
 
     # the tuned path: staged kernel in the chosen precision, autotuned, on the
-    # learned blocking when it is faster than the reference's
+    # reference's blocking or on the learned one, whichever reaches the test
+    # RMSE target of the learning regime first (epoch time alone would favour
+    # the learned blocking, whose unpadded epochs do fewer updates)
+    ecfg, elearn = TRAJ_EPOCHS.get(args.workload, (10, 30))
+    if args.traj_epochs:
+        ecfg, elearn = args.traj_epochs
     learned = None
     model = None
     tune = None
+    traj_tl = None
     ctx = ctx_on(sched_h, dtype, mode)
     sched = sched_h
     ph.mark("context_tuned_reference")
@@ -456,22 +462,32 @@ def run_gpu(args):
         tune_l = ctx_l.autotune(2) if not args.no_tune else None
         ms_l = _epoch_ms(ctx_l, 3)
         upd_l, upd_h = sched_l.summary.scheduled_updates, sm.scheduled_updates
-        kept = ms_l < ms_h
-        learned = {"kept": bool(kept), "model_r2": r2, "samples": int(len(y)),
+        tr_h = _trajectory(ctx, w, elearn, rates=(LEARN["lr"], LEARN["reg"]), train_every=5)
+        tr_l = _trajectory(ctx_l, w, elearn, rates=(LEARN["lr"], LEARN["reg"]), train_every=5)
+        target = 1.01 * min(tr_h[-1][2], tr_l[-1][2])
+        _, t_h = _time_to(tr_h, target)
+        _, t_l = _time_to(tr_l, target)
+        kept = t_l is not None and (t_h is None or t_l < t_h)
+        learned = {"kept": bool(kept), "judge": "device time to 1.01 x the better final test RMSE of the two, "
+                                                "learning regime, %d epochs" % elearn,
+                   "model_r2": r2, "samples": int(len(y)),
                    "epoch_ms_learned": ms_l, "epoch_ms_reference": ms_h,
                    "updates_per_epoch_learned": int(upd_l), "updates_per_epoch_reference": int(upd_h),
+                   "time_to_target_ms_learned": t_l, "time_to_target_ms_reference": t_h,
+                   "final_test_rmse_learned": tr_l[-1][2], "final_test_rmse_reference": tr_h[-1][2],
                    "blocks_learned": int(sched_l.summary.num_blocks), "groups_learned": int(sched_l.summary.num_groups),
                    "build_seconds_learned": round(sum(sched_l.summary.build_seconds), 2)}
         log("learned blocking: %d blocks, %d groups, %d updates/epoch, %.3f ms/epoch vs reference %.3f ms/epoch "
-            "(%d updates); model R2 %.3f on %d blocks; kept %d" % (sched_l.summary.num_blocks,
-                                                                   sched_l.summary.num_groups, upd_l, ms_l, ms_h,
-                                                                   upd_h, r2, len(y), kept))
+            "(%d updates); model R2 %.3f on %d blocks; learning regime final RMSE %.5f vs %.5f; kept %d"
+            % (sched_l.summary.num_blocks, sched_l.summary.num_groups, upd_l, ms_l, ms_h, upd_h, r2, len(y),
+               tr_l[-1][2], tr_h[-1][2], kept))
         if kept:
             ctx.close()
-            ctx, sched, tune = ctx_l, sched_l, tune_l
+            ctx, sched, tune, traj_tl = ctx_l, sched_l, tune_l, tr_l
         else:
             ctx_l.close()
             sched_l.close()
+            traj_tl = tr_h
         ph.mark("judge")
     upd_per_step = sched.summary.scheduled_updates
     rm0 = ctx.eval(bg.TEST).rmse
@@ -502,13 +518,11 @@ def run_gpu(args):
     for p_ in pinned:
         p_.free()
     ph.mark("e2e")
-    ecfg, elearn = TRAJ_EPOCHS.get(args.workload, (10, 30))
-    if args.traj_epochs:
-        ecfg, elearn = args.traj_epochs
-    traj_t = traj_tl = None
+    traj_t = None
     if not args.no_plain:
         traj_t = _trajectory(ctx, w, ecfg)
-        traj_tl = _trajectory(ctx, w, elearn, rates=(LEARN["lr"], LEARN["reg"]), train_every=5)
+        if traj_tl is None:
+            traj_tl = _trajectory(ctx, w, elearn, rates=(LEARN["lr"], LEARN["reg"]), train_every=5)
         ph.mark("trajectories_tuned")
     ctx.close()
 

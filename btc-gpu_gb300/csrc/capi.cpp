@@ -81,7 +81,7 @@ struct btc_ctx {
     int nhot[3] = {0, 0, 0};
     unsigned epoch = 0;
     int* status = nullptr;
-    int st_cap = 0, st_wave = 0, st_grid = 0, st_block = 256, st_G = 0, st_NV = 0;
+    int st_cap = 0, st_wave = 0, st_grid = 0, st_block = 256, st_G = 0, st_NV = 0, st_repeat = 0;
     size_t st_smem = 0;
     std::vector<float> tile_feat;  // BTC_TILE_FEATURES per tile
     std::vector<int> h_tile0, h_ntiles;  // host copy of each slot's tiles
@@ -618,8 +618,21 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
         if (c->st_cap < 3)
             return BTC_ERR_UNSUPPORTED;  // one entry needs three staged rows
         btc::TileSet ts;
-        btc::build_tiles(s, txyz, tval, cfg.I, cfg.J, cfg.K, c->st_cap, c->st_wave, 16,
-                         cfg.row_repeat > 0 ? cfg.row_repeat : 16,
+        // Most entries of one row per tile.  A tile's entries all read the
+        // rows as they were when it started, so a row met c times takes a
+        // Jacobi step of gain ~ lr * c * |other rows|^2; measured on a
+        // skewed 50M-entry tensor (R 32), c = 64 held at lr 0.005 and 0.01
+        // and diverged at 0.02, c = 16 held at 0.02, uncapped tiles (c in the
+        // hundreds) diverged at 0.01 and at 0.005 once the factors had grown.
+        // The default is the power of two at or below 0.32 / lr, in [16, 512].
+        int repeat = cfg.row_repeat;
+        if (repeat <= 0) {
+            repeat = 16;
+            while (repeat < 512 && (double)(repeat * 2) * cfg.lr <= 0.32 + 1e-12)
+                repeat *= 2;
+        }
+        c->st_repeat = repeat;
+        btc::build_tiles(s, txyz, tval, cfg.I, cfg.J, cfg.K, c->st_cap, c->st_wave, 16, repeat,
                          c->dtype == BTC_DTYPE_F64, ts, default_threads(cfg));
         std::vector<int> t0(nslots), tn(nslots);
         for (int k = 0; k < nslots; k++) {

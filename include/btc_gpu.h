@@ -98,7 +98,8 @@ typedef struct btc_config {
     int32_t chunk;                  /* entries per Hogwild work item, 0 = auto */
     int32_t host_threads;           /* builder threads, 0 = hardware concurrency */
     int32_t ctas_per_sm;            /* staged kernel: CTAs sharing one SM's shared memory, 0 = auto */
-    int32_t row_repeat;             /* staged kernel: most entries of one row in a tile, 0 = 16 */
+    int32_t row_repeat;             /* staged kernel: most entries of one row in a tile; 0 = the
+                                       power of two at or below 0.32 / lr, in [16, 512] */
     int32_t reserved[5];
 } btc_config;
 
@@ -203,6 +204,8 @@ btc_status btc_ctx_get_factors(btc_ctx *ctx, int32_t mode, double *host);
  * rows that decay from their value at write time stay the ones chosen at
  * creation. */
 btc_status btc_ctx_set_rates(btc_ctx *ctx, double lr, double reg);
+/* (In staged contexts the tiles' row_repeat bound was chosen for the
+ * creation lr: a much larger lr wants a context built with it.) */
 /* U(lo, hi) init from a counter-based generator (seed, mode, row, col) */
 btc_status btc_ctx_init_factors(btc_ctx *ctx, uint64_t seed, double lo, double hi);
 /* One epoch: the reference's GPUs<<<max_parallel, thread_size>>> launch
