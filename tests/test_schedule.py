@@ -357,3 +357,36 @@ def test_learned_blocking_schedules_every_entry_once_in_conflict_free_groups(dim
     assert np.array_equal(s1.boxes(), boxes)
     for x, y in zip(s1.groups(), s.groups()):
         assert np.array_equal(x, y)
+
+
+def test_config1_blocking_equals_the_pinned_reference_schedule(tmp_path):
+    """The 1M-entry config-1 input (900k train entries): the product builder's
+    schedule -- groups, slots, coe weights, every slot's entries in order --
+    and its block_parallel.txt hash to the digests of the reference's own
+    block.cu output committed by tests/golden/make_c1_pin.py."""
+    import hashlib
+    import json
+
+    import make_c1_pin as pin_mod
+
+    with open(os.path.join(ROOT, "tests", "golden", "c1_pin.json")) as f:
+        pin = json.load(f)
+    spec = dict(pin["spec"])
+    I, J, K, nnz = spec.pop("I"), spec.pop("J"), spec.pop("K"), spec.pop("nnz")
+    tx, tv, _, _ = bg.gen_tensor(I, J, K, nnz, **spec)
+    tx, tv = bg.shuffle(tx, tv)
+    assert len(tv) == pin["train_nnz"]
+    cfg = bg.config(I=I, J=J, K=K, block_s=pin["block_s"], parallel_sequence_size=pin["parallel_sequence_size"],
+                    resident_blocks=-1)
+    s = bg.Schedule(cfg, tx)
+    off, ids, coe = s.groups()
+    assert len(ids) == pin["slots"] and len(off) - 1 == pin["groups"]
+    slots = []
+    for k in range(len(ids)):
+        e = s.block_entries(int(ids[k]))
+        slots.append(dict(id=int(ids[k]), nnz=len(e), coe=tuple(coe[k]), xyz=tx[e].tolist()))
+    num_bs = [int(off[g + 1] - off[g]) for g in range(len(off) - 1)]
+    assert pin_mod.digest(pin_mod.canonical(num_bs, slots)) == pin["schedule_sha256"]
+    rep = tmp_path / "block_parallel.txt"
+    s.write_report(str(rep))
+    assert hashlib.sha256(rep.read_bytes()).hexdigest() == pin["report_sha256"]
