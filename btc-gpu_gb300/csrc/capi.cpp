@@ -480,8 +480,8 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
         lf_coe.assign(3 * lf_slots.size(), 1.0);
     }
     const bool lf = c->cfg.mode == BTC_MODE_LOCKFREE;
-    const std::vector<int32_t>& slot_block = lf ? lf_slots : slot_block;
-    const std::vector<double>& slot_coe = lf ? lf_coe : slot_coe;
+    const std::vector<int32_t>& slot_block = lf ? lf_slots : s.slot_block;
+    const std::vector<double>& slot_coe = lf ? lf_coe : s.slot_coe;
     const btc_config& cfg = c->cfg;
     CK(cudaSetDevice(cfg.device));
     cudaDeviceProp prop;

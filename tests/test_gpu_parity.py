@@ -365,7 +365,9 @@ def test_lockfree_f64_equals_the_serial_lockfree_rule(case_name, R):
     for epoch in range(3):
         upd = sched.lf_epoch(val, R, LR, REG, *ref)
         st = ctx.train_epoch()
-        assert st.updates == upd == len(val) and st.device_status == 0
+        # every block once; the duplicating re-split (Q4) can leave an entry
+        # in two blocks, so an epoch can hold more updates than entries
+        assert st.updates == upd >= len(val) and st.device_status == 0
         for m in range(3):
             got = ctx.get_factors(m)
             assert np.array_equal(got, ref[m]), (epoch, m, np.abs(got - ref[m]).max())
@@ -394,3 +396,33 @@ def test_lockfree_has_no_bf16_form():
     with pytest.raises(bg.BtcError) as e:
         _ctx(c, xyz, val, 8, bg.BF16, bg.LOCKFREE)
     assert e.value.status == 7  # BTC_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("dtype", [bg.F32, bg.BF16])
+def test_staged_stays_stable_where_the_factors_grow(dtype):
+    """No regularisation and lr 0.02 on a skewed tensor: the factors grow from
+    U(0, 0.1) to the data's scale within a few epochs.  Tiles that let a hot
+    row take hundreds of snapshot updates diverged here; with the row bound
+    (16 per tile at this rate) the staged paths stay finite and learn, as
+    the plain Hogwild path does."""
+    I, J, K, R = 100000, 100000, 10000, 32
+    tx, tv, sx, sv = bg.gen_tensor(I, J, K, 5_000_000, zipf=(1.2, 1.2, 1.2), gt_rank=16, noise_std=0.05,
+                                   train_frac=0.9, seed=23)
+    tx, tv = bg.shuffle(tx, tv)
+    out = {}
+    for name, dt, md in (("staged", dtype, bg.STAGED), ("plain", bg.F32, bg.HOGWILD)):
+        cfg = bg.config(I=I, J=J, K=K, rank=R, lr=0.02, reg=0.0, block_s=2048, parallel_sequence_size=8,
+                        dtype=dt, mode=md)
+        ctx = bg.Context(cfg, bg.Schedule(cfg, tx), tx, tv, sx, sv)
+        ctx.init_factors(3, 0.0, 0.1)
+        r0 = ctx.eval(bg.TEST).rmse
+        rs = []
+        for _ in range(15):
+            assert ctx.train_epoch().device_status == 0
+            rs.append(ctx.eval(bg.TEST).rmse)
+        ctx.close()
+        out[name] = (r0, rs)
+        assert np.isfinite(rs).all(), (name, rs)
+    r0, rs = out["staged"]
+    assert rs[-1] < 0.6 * r0, out  # it learned
+    assert rs[-1] < 2.0 * out["plain"][1][-1], out
