@@ -76,6 +76,10 @@ WORKLOADS = {
                noise=0.05, train=0.95, R=32, lr=0.005, reg=0.02, epochs=10,
                desc="largest single tensor: I=J=1M K=100k, 1B nnz Zipf(1.3) per mode, rank-32 GT + N(0,0.05), "
                     "95/5 split, R=32, lr 0.005, lambda 0.02"),
+    "c2s": dict(I=100000, J=100000, K=10000, nnz=10_000_000, zipf=(1.2, 1.2, 1.2), gt_rank=16, noise=0.05,
+                train=0.9, R=32, lr=0.005, reg=0.02, epochs=20,
+                desc="profiling case of the C2 shape: I=J=100k K=10k, 10M nnz Zipf(1.2) per mode, rank-16 GT + "
+                     "N(0,0.05), 90/10 split, R=32, lr 0.005, lambda 0.02"),
     "small": dict(I=20000, J=20000, K=5000, nnz=2_000_000, zipf=(1.2, 1.2, 1.2), gt_rank=16, noise=0.05,
                   train=0.9, R=32, lr=0.005, reg=0.02, epochs=10,
                   desc="small skewed: I=J=20k K=5k, 2M nnz Zipf(1.2), R=32"),
@@ -607,12 +611,12 @@ def run_gpu(args):
 
 
 def run_c4(args):
-    """64 independent tensors: one persistent launch + CUDA graph per epoch,
-    against the same tensors launched one after another."""
+    """64 independent tensors: one persistent launch + CUDA graph per epoch
+    (BF16 and FP32), against the same tensors launched one after another,
+    and per-tensor time to the plain FP32 path's test RMSE."""
     import btc_gpu as bg
 
     rng = np.random.default_rng(SEED + 4)
-    dtype = {"f32": bg.F32, "bf16": bg.BF16}.get(args.dtype, bg.BF16)
     specs = []
     for i in range(64):
         dims = [int(v) for v in np.exp(rng.uniform(np.log(500), np.log(50000), 3))]
@@ -627,69 +631,107 @@ def run_c4(args):
         bg.shuffle(tx, tv)
         cfgk = dict(I=dims[0], J=dims[1], K=dims[2], rank=R, lr=0.01, reg=0.01, block_s=2048,
                     parallel_sequence_size=8)
-        sched = bg.Schedule(bg.config(mode=bg.STAGED, dtype=dtype, **cfgk), tx)
+        sched = bg.Schedule(bg.config(mode=bg.STAGED, dtype=bg.BF16, **cfgk), tx)
         rr = np.random.default_rng(SEED + 200 + i)
         init = [rr.uniform(0.0, 0.1, (n, R)) for n in dims]
         tensors.append((cfgk, sched, (tx, tv, sx, sv), init))
     log("c4: 64 tensors, %d train entries, built in %.1fs" % (sum(len(t[2][1]) for t in tensors), time.time() - t0))
 
-    def contexts(dt, md):
+    def contexts(dt, md, rates=None):
         out = []
         for cfgk, sched, data, init in tensors:
             c = bg.Context(bg.config(mode=md, dtype=dt, **cfgk), sched, *data)
             for m in range(3):
                 c.set_factors(m, init[m])
+            if rates:
+                c.set_rates(*rates)
             out.append(c)
         return out
 
+    def reset(cs):
+        for c, t in zip(cs, tensors):
+            for m in range(3):
+                c.set_factors(m, t[3][m])
+
     upd = sum(t[1].summary.scheduled_updates for t in tensors)
-    res = {}
-    # one launch per epoch for all tensors, captured as a CUDA graph
-    cs = contexts(dtype, bg.STAGED)
-    b = bg.Batch(cs)
-    b.train_epochs(args.warmup, graph=True)
-    st = b.train_epochs(args.steps, graph=True)
-    res["batched_graph"] = upd * args.steps / (st.kernel_ms / 1e3)
-    st_ng = b.train_epochs(args.steps, graph=False)
-    res["batched_no_graph"] = upd * args.steps / (st_ng.kernel_ms / 1e3)
-    # test RMSE after the same number of epochs from the same init, batched vs plain
-    epochs_cmp = 10
-    for c, t in zip(cs, tensors):
-        for m in range(3):
-            c.set_factors(m, t[3][m])
-    b.train_epochs(epochs_cmp, graph=True)
-    rm_batch = [c.eval(bg.TEST).rmse for c in cs]
-    b.close()
-    # the same kernel, one launch per tensor, one tensor after another
-    seq_ms = 0.0
-    for c in cs:
-        c.train_epochs(1)
-        seq_ms += c.train_epochs(args.steps).kernel_ms
-    res["sequential_staged"] = upd * args.steps / (seq_ms / 1e3)
-    for c in cs:
-        c.close()
-    # the plain FP32 path run sequentially per tensor
+    res, st_main = {}, None
+    epochs_cmp = 20
+    rm_batch = {}
+    traj = {}
+    for name, dt in (("bf16", bg.BF16), ("f32", bg.F32)):
+        cs = contexts(dt, bg.STAGED)
+        b = bg.Batch(cs)
+        b.train_epochs(args.warmup, graph=True)
+        st = b.train_epochs(args.steps, graph=True)
+        res["batched_graph_" + name] = upd * args.steps / (st.kernel_ms / 1e3)
+        if name == "bf16":
+            st_main = st
+            st_ng = b.train_epochs(args.steps, graph=False)
+            res["batched_no_graph_bf16"] = upd * args.steps / (st_ng.kernel_ms / 1e3)
+        b.close()
+        # per-tensor test RMSE after every batched epoch from the same init
+        reset(cs)
+        b = bg.Batch(cs)
+        tr, t_ms = [], 0.0
+        for _ in range(epochs_cmp):
+            t_ms += b.train_epochs(1, graph=True).kernel_ms
+            tr.append((t_ms, [c.eval(bg.TEST).rmse for c in cs]))
+        b.close()
+        traj[name] = tr
+        rm_batch[name] = tr[-1][1]
+        if name == "bf16":
+            seq_ms = 0.0
+            for c in cs:
+                c.train_epochs(1)
+                seq_ms += c.train_epochs(args.steps).kernel_ms
+            res["sequential_staged_bf16"] = upd * args.steps / (seq_ms / 1e3)
+        for c in cs:
+            c.close()
+    # the plain FP32 path, tensor after tensor: throughput and per-tensor RMSE
     cp = contexts(bg.F32, bg.HOGWILD)
+    plain_tr = []
     for c in cp:
-        c.train_epochs(epochs_cmp)
-    rm_plain = [c.eval(bg.TEST).rmse for c in cp]
+        t_ms, rs = 0.0, []
+        for _ in range(epochs_cmp):
+            t_ms += c.train_epoch().kernel_ms
+            rs.append((t_ms, c.eval(bg.TEST).rmse))
+        plain_tr.append(rs)
     pl_ms = 0.0
     for c in cp:
         pl_ms += c.train_epochs(args.steps).kernel_ms
     res["sequential_plain_fp32"] = upd * args.steps / (pl_ms / 1e3)
     for c in cp:
         c.close()
-    line = {"metric": "aggregate nnz-updates/s, 64 tensors", "value": res["batched_graph"], "unit": "updates/s",
+    # per tensor: device time to 1.01 x its plain run's final test RMSE; the
+    # batched time is the whole batch's (every tensor advances in each launch)
+    per = []
+    for i in range(len(tensors)):
+        target = plain_tr[i][-1][1] * 1.01
+        tp = next((t for t, r in plain_tr[i] if r <= target), None)
+        tb = next((t for t, rs in traj["bf16"] if rs[i] <= target), None)
+        per.append({"nnz": int(specs[i][1]), "rank": specs[i][2], "plain_ms": tp, "batched_bf16_ms": tb,
+                    "plain_final_rmse": plain_tr[i][-1][1], "batched_bf16_final_rmse": rm_batch["bf16"][i],
+                    "batched_f32_final_rmse": rm_batch["f32"][i]})
+    reached = [p for p in per if p["batched_bf16_ms"] is not None]
+    seq_total = sum(p["plain_ms"] or 0.0 for p in per)
+    rel = lambda a, b: abs(a - b) / b  # noqa: E731
+    line = {"metric": "aggregate nnz-updates/s, 64 tensors", "value": res["batched_graph_bf16"], "unit": "updates/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": st.kernel_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
+            "ms_per_step": st_main.kernel_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
             "config": {"workload": "64 tensors, dims log-uniform [500, 50k], nnz log-uniform [1e4, 5e6], "
-                                   "Zipf(1.1), R in {8,16,32}, rank-8 GT + N(0,0.01)",
-                       "updates_per_epoch": int(upd)},
-            "gpu_launches": st.launches, "paths": res,
-            "speedup_vs_sequential_plain": res["batched_graph"] / res["sequential_plain_fp32"],
-            "speedup_vs_sequential_staged": res["batched_graph"] / res["sequential_staged"],
-            "max_rel_rmse_vs_plain": float(max(abs(a - p_) / p_ for a, p_ in zip(rm_batch, rm_plain)))}
+                                   "Zipf(1.1), R in {8,16,32}, rank-8 GT + N(0,0.01), lr 0.01, lambda 0.01",
+                       "name": "c4"},
+            "setup": {"updates_per_epoch": int(upd)},
+            "gpu_launches": st_main.launches, "paths": res,
+            "speedup_vs_sequential_plain": res["batched_graph_bf16"] / res["sequential_plain_fp32"],
+            "speedup_vs_sequential_staged": res["batched_graph_bf16"] / res["sequential_staged_bf16"],
+            "bf16_vs_f32_batched": res["batched_graph_bf16"] / res["batched_graph_f32"],
+            "max_rel_rmse_vs_plain": {k: float(max(rel(a, p["plain_final_rmse"]) for a, p in zip(v, per)))
+                                      for k, v in rm_batch.items()},
+            "time_to_rmse": {"epochs": epochs_cmp, "tensors_reaching_target": len(reached),
+                             "batched_bf16_ms_all_tensors": max((p["batched_bf16_ms"] for p in reached), default=None),
+                             "plain_ms_sum_over_tensors": seq_total, "per_tensor": per}}
     print(json.dumps(line), flush=True)
     return 0
 
