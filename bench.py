@@ -48,6 +48,7 @@ between strata); --gpus N under torchrun runs N independent replicas
 import argparse
 import json
 import os
+import resource
 import statistics
 import subprocess
 import sys
@@ -583,7 +584,8 @@ def run_gpu(args):
                           "l2": "inputs larger than L2: entry stream %.2f GB per epoch; factor rows (%.0f MB) stay "
                                 "L2-resident as in a real run" % (upd_per_step * 16 / 1e9, sum(
                                     n * w["R"] * s_f for n in (w["I"], w["J"], w["K"])) / 1e6),
-                          "phases_s": ph.d},
+                          "phases_s": ph.d,
+                          "host_peak_rss_gb": round(resource.getrusage(resource.RUSAGE_SELF).ru_maxrss / 2 ** 20, 1)},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": st.launches,
                 "train_nnz_per_s": len(tv) * args.steps * world / (ms / 1000.0),
                 "test_rmse": {"after_warmup": rm0, "after_timed": rm1, "e2e_last": met.rmse}}
