@@ -360,6 +360,67 @@ def _epoch_ms(ctx, n):
     return ctx.train_epochs(n).kernel_ms / n
 
 
+def judge_learned(w, dtype, mode, device, elearn, args):
+    """The learned blocking against the reference's, judged on the workload's
+    first REF_SAMPLE_NNZ cells (the whole workload when it is smaller): the
+    block cost model is trained on block timings a profiled epoch records on
+    the reference blocking, the learned schedule is built with it, and both
+    run the learning-regime trajectory; the learned blocking is kept when it
+    reaches 1.01 x the better final test RMSE sooner."""
+    import btc_gpu as bg
+
+    m = min(w["nnz"], REF_SAMPLE_NNZ)
+    tx, tv, sx, sv = bg.gen_tensor(w["I"], w["J"], w["K"], m, zipf=w["zipf"], gt_rank=w["gt_rank"], gt_std=0.5,
+                                   noise_std=w["noise"], train_frac=w["train"], seed=SEED)
+    bg.shuffle(tx, tv)
+    cfg = cfg_for(w, dtype, mode, device=device)
+    init = init_factors(w)
+
+    def ctx_on(sched):
+        c = bg.Context(cfg, sched, tx, tv, sx, sv)
+        for q in range(3):
+            c.set_factors(q, init[q])
+        c.train_epochs(args.warmup)
+        if not args.no_tune:
+            c.autotune(2)
+        return c
+
+    sh = bg.Schedule(cfg, tx)
+    ch = ctx_on(sh)
+    ms_h = _epoch_ms(ch, 3)
+    f, y = ch.block_profile()
+    model = bg.MLP(n_in=bg.BLOCK_FEATURES, seed=7)
+    loss = model.train(f, y, 400)
+    r2 = 1.0 - loss / max(1e-12, float(np.var(y)))
+    t = time.time()
+    sl = bg.Schedule(cfg, tx, learned=True, model=model)
+    build_s = time.time() - t
+    cl = ctx_on(sl)
+    ms_l = _epoch_ms(cl, 3)
+    tr_h = _trajectory(ch, w, elearn, rates=(LEARN["lr"], LEARN["reg"]), train_every=5)
+    tr_l = _trajectory(cl, w, elearn, rates=(LEARN["lr"], LEARN["reg"]), train_every=5)
+    target = 1.01 * min(tr_h[-1][2], tr_l[-1][2])
+    _, t_h = _time_to(tr_h, target)
+    _, t_l = _time_to(tr_l, target)
+    kept = t_l is not None and (t_h is None or t_l < t_h)
+    rep = {"kept": bool(kept),
+           "judge": "on the first %d cells: device time to 1.01 x the better final test RMSE of the two, learning "
+                    "regime, %d epochs" % (m, elearn),
+           "model_r2": r2, "samples": int(len(y)), "epoch_ms_learned": ms_l, "epoch_ms_reference": ms_h,
+           "updates_per_epoch_learned": int(sl.summary.scheduled_updates),
+           "updates_per_epoch_reference": int(sh.summary.scheduled_updates),
+           "time_to_target_ms_learned": t_l, "time_to_target_ms_reference": t_h,
+           "final_test_rmse_learned": tr_l[-1][2], "final_test_rmse_reference": tr_h[-1][2],
+           "blocks_learned": int(sl.summary.num_blocks), "groups_learned": int(sl.summary.num_groups),
+           "build_seconds_learned": round(build_s, 2)}
+    log("learned blocking on %d cells: %.3f vs %.3f ms/epoch (%d vs %d updates), model R2 %.3f; learning regime "
+        "final RMSE %.5f vs %.5f; kept %d" % (m, ms_l, ms_h, sl.summary.scheduled_updates,
+                                              sh.summary.scheduled_updates, r2, tr_l[-1][2], tr_h[-1][2], kept))
+    ch.close()
+    cl.close()
+    return rep, model, kept
+
+
 def oracle_check(w, name, model, tuned_learned, dtype):
     """One epoch of the tuned and the plain configuration on the workload's
     first REF_SAMPLE_NNZ cells against the serial FP64 replay of the same
@@ -453,47 +514,16 @@ def run_gpu(args):
         tune = ctx.autotune(2)
         ph.mark("autotune")
     if mode == bg.STAGED and not args.no_learned:
-        ms_h = _epoch_ms(ctx, 3)
-        f, y = ctx.block_profile()
-        model = bg.MLP(n_in=bg.BLOCK_FEATURES, seed=7)
-        loss = model.train(f, y, 400)
-        r2 = 1.0 - loss / max(1e-12, float(np.var(y)))
-        ph.mark("block_profile+model")
-        sched_l = bg.Schedule(cfg, tx, learned=True, model=model)
-        ph.mark("schedule_learned")
-        ctx_l = ctx_on(sched_l, dtype, mode)
-        ph.mark("context_tuned_learned")
-        ctx_l.train_epochs(args.warmup)
-        tune_l = ctx_l.autotune(2) if not args.no_tune else None
-        ms_l = _epoch_ms(ctx_l, 3)
-        upd_l, upd_h = sched_l.summary.scheduled_updates, sm.scheduled_updates
-        tr_h = _trajectory(ctx, w, elearn, rates=(LEARN["lr"], LEARN["reg"]), train_every=5)
-        tr_l = _trajectory(ctx_l, w, elearn, rates=(LEARN["lr"], LEARN["reg"]), train_every=5)
-        target = 1.01 * min(tr_h[-1][2], tr_l[-1][2])
-        _, t_h = _time_to(tr_h, target)
-        _, t_l = _time_to(tr_l, target)
-        kept = t_l is not None and (t_h is None or t_l < t_h)
-        learned = {"kept": bool(kept), "judge": "device time to 1.01 x the better final test RMSE of the two, "
-                                                "learning regime, %d epochs" % elearn,
-                   "model_r2": r2, "samples": int(len(y)),
-                   "epoch_ms_learned": ms_l, "epoch_ms_reference": ms_h,
-                   "updates_per_epoch_learned": int(upd_l), "updates_per_epoch_reference": int(upd_h),
-                   "time_to_target_ms_learned": t_l, "time_to_target_ms_reference": t_h,
-                   "final_test_rmse_learned": tr_l[-1][2], "final_test_rmse_reference": tr_h[-1][2],
-                   "blocks_learned": int(sched_l.summary.num_blocks), "groups_learned": int(sched_l.summary.num_groups),
-                   "build_seconds_learned": round(sum(sched_l.summary.build_seconds), 2)}
-        log("learned blocking: %d blocks, %d groups, %d updates/epoch, %.3f ms/epoch vs reference %.3f ms/epoch "
-            "(%d updates); model R2 %.3f on %d blocks; learning regime final RMSE %.5f vs %.5f; kept %d"
-            % (sched_l.summary.num_blocks, sched_l.summary.num_groups, upd_l, ms_l, ms_h, upd_h, r2, len(y),
-               tr_l[-1][2], tr_h[-1][2], kept))
+        learned, model, kept = judge_learned(w, dtype, mode, local, elearn, args)
+        ph.mark("learned_judge")
         if kept:
+            sched_l = bg.Schedule(cfg, tx, learned=True, model=model)
+            ctx_l = ctx_on(sched_l, dtype, mode)
+            ctx_l.train_epochs(args.warmup)
+            tune_l = ctx_l.autotune(2) if not args.no_tune else None
             ctx.close()
-            ctx, sched, tune, traj_tl = ctx_l, sched_l, tune_l, tr_l
-        else:
-            ctx_l.close()
-            sched_l.close()
-            traj_tl = tr_h
-        ph.mark("judge")
+            ctx, sched, tune = ctx_l, sched_l, tune_l
+            ph.mark("learned_blocking_full")
     upd_per_step = sched.summary.scheduled_updates
     rm0 = ctx.eval(bg.TEST).rmse
     clocks = Clocks(local)
