@@ -135,11 +135,24 @@ __device__ __forceinline__ void cp16(void* smem_dst, const void* gsrc)
 }
 __device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-// One work unit of one tensor: slots [unit_off[unit], unit_off[unit+1]),
-// tile by tile.  MASK allows a row shorter than G*NV*VN elements (the lanes
-// past the padded rank stay idle), so one shape serves every rank of a batch.
-template <typename T, int GC, int NV, bool BF, bool MASK>
-__device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned char* smem)
+// No-op hooks: a tile processed on its own (the batched kernel's path).
+struct NoHook {
+    __device__ __forceinline__ void after_stage() const {}
+    __device__ __forceinline__ void after_errors() const {}
+};
+
+// One tile t of slot `slot`: header h, staged row ids in `rid` (already
+// filled when rid_ready, else loaded here).  MASK allows a row shorter than
+// G*NV*VN elements (the lanes past the padded rank stay idle), so one shape
+// serves every rank of a batch.  hook.after_stage() runs once the tile is
+// staged and visible to the whole CTA, hook.after_errors() once the errors
+// are: a caller uses them to fetch the next tile's header and row ids while
+// this tile computes.  fence: the slot's next tile follows on this CTA and
+// must see this tile's adds.
+template <typename T, int GC, int NV, bool BF, bool MASK, typename Hook>
+__device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem, const TileHdr& h, int t,
+                                        int slot, T cx, T cy, T cz, int* rid, bool rid_ready, bool fence,
+                                        unsigned seed, const Hook& hook)
 {
     using V = typename SV<T>::V;
     constexpr int VN = SV<T>::N;
@@ -154,7 +167,6 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
     T* S = reinterpret_cast<T*>(smem);
     int4* ent = reinterpret_cast<int4*>(smem + L.ent);
     T* err = reinterpret_cast<T*>(smem + L.err);
-    int* rid = reinterpret_cast<int*>(smem + L.rid);
     unsigned short* csr = reinterpret_cast<unsigned short*>(smem + L.csr);
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
@@ -164,282 +176,396 @@ __device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned
     T* const FC = static_cast<T*>(a.C);
     const T reg = (T)a.reg;
     const int vpr = Rp / VN;
+    unsigned long long t_start = 0;
+    if (a.tile_ns && tid == 0)
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
+    const int nv = h.nrows * vpr;
+    const int nxy = h.nx + h.ny;
+    // rounding stream of this visit of this tile (BF16)
+    const unsigned tile_bits = BF ? mix3(seed, (unsigned)t, (unsigned)slot) : 0u;
+    // the first owner segment of this lane group, fetched now so that
+    // its latency hides behind staging and the errors
+    const int seg_stride = nwarps * EPW;
+    unsigned sg_next = 0;
+    if (warp * EPW + sub < h.nseg)
+        sg_next = __ldg(&a.segs[h.soff + warp * EPW + sub]);
+    // 1. stage: rows, entries and CSR lists, all as 16-byte async copies
+    //    (BF16 rows are widened to FP32 through registers)
+    if constexpr (BF) {
+        const int cpr = Rp / 8;  // 16-byte chunks per BF16 row
+        const int nc = h.nrows * cpr;
+        unsigned short* Sb = reinterpret_cast<unsigned short*>(smem);
+        for (int i = tid; i < nc; i += blockDim.x) {
+            const int r = i / cpr, c = i - r * cpr;
+            // the global row, or ~(master index | FAST) for a row with an FP32 master
+            // (from shared memory when the caller prefetched it)
+            const int g = rid_ready ? rid[r] : __ldg(&a.rows[h.roff + r]);
+            const int m = r < h.nx ? 0 : (r < nxy ? 1 : 2);
+            if (!rid_ready && c == 0)
+                rid[r] = g;
+            if (g < 0) {
+                const float* mm = m == 0 ? a.master[0] : (m == 1 ? a.master[1] : a.master[2]);
+                const size_t hm = (size_t)(~g & (FAST - 1));
+                const float4 v0 = __ldcg(reinterpret_cast<const float4*>(mm + hm * Rp + c * 8));
+                const float4 v1 = __ldcg(reinterpret_cast<const float4*>(mm + hm * Rp + c * 8 + 4));
+                uint4 q;
+                q.x = pack_bf16x2_rn(v0.x, v0.y);
+                q.y = pack_bf16x2_rn(v0.z, v0.w);
+                q.z = pack_bf16x2_rn(v1.x, v1.y);
+                q.w = pack_bf16x2_rn(v1.z, v1.w);
+                *reinterpret_cast<uint4*>(Sb + (size_t)r * Rp + c * 8) = q;
+            } else {
+                const unsigned short* Fm = static_cast<const unsigned short*>(
+                    m == 0 ? a.A : (m == 1 ? a.B : a.C));
+                cp16(Sb + (size_t)r * Rp + c * 8, Fm + (size_t)g * Rp + c * 8);
+            }
+        }
+    }
+    for (int i = tid; i < (BF ? 0 : nv); i += blockDim.x) {
+        const int r = i / vpr, c = i - r * vpr;
+        const int g0 = rid_ready ? rid[r] : __ldg(&a.rows[h.roff + r]);  // the global row, or ~row (FAST)
+        const int g = g0 < 0 ? ~g0 : g0;
+        if constexpr (BF) {
+            // rows stay BF16 in shared memory: 16-byte chunks of 8
+            // elements, copied as they are; hot rows are rounded from
+            // their FP32 masters
+            (void)c;
+        }
+        if constexpr (!BF) {
+            if (!rid_ready && c == 0)
+                rid[r] = g0;
+            const T* Fm = r < h.nx ? FA : (r < nxy ? FB : FC);
+            cp16(reinterpret_cast<V*>(S) + i, reinterpret_cast<const V*>(Fm + (size_t)g * Rp) + c);
+        }
+    }
+    for (int i = tid; i < h.n; i += blockDim.x)
+        cp16(ent + i, a.ent + h.eoff + i);
+    const int nc = (3 * h.n + 7) >> 3;
+    for (int i = tid; i < nc; i += blockDim.x)
+        cp16(csr + 8 * i, a.csr + h.coff + 8 * i);
+    cp_wait_all();
+    __syncthreads();
+    hook.after_stage();
+    // 2. errors
+    for (int e0 = warp * EPW; e0 < h.n; e0 += nwarps * EPW) {
+        const int e = e0 + sub;
+        const bool act = e < h.n;
+        T p = T(0);
+        int4 q = make_int4(0, 0, 0, 0);
+        if (act) {
+            q = ent[e];
+            const size_t rx = (size_t)(q.x & 0xffff) * Rp, ry = (size_t)((unsigned)q.x >> 16) * Rp,
+                         rz = (size_t)q.y * Rp;
+#pragma unroll
+            for (int j = 0; j < NV; j++) {
+                const int o = (j * G + gl) * VN;
+                if (MASK && o >= Rp)
+                    continue;
+                V vx, vy, vz;
+                if constexpr (BF) {
+                    const unsigned short* Sb = reinterpret_cast<const unsigned short*>(smem);
+                    vx = ld_bf4(Sb + rx + o);
+                    vy = ld_bf4(Sb + ry + o);
+                    vz = ld_bf4(Sb + rz + o);
+                } else {
+                    vx = *reinterpret_cast<const V*>(S + rx + o);
+                    vy = *reinterpret_cast<const V*>(S + ry + o);
+                    vz = *reinterpret_cast<const V*>(S + rz + o);
+                }
+                const T* ax = reinterpret_cast<const T*>(&vx);
+                const T* ay = reinterpret_cast<const T*>(&vy);
+                const T* az = reinterpret_cast<const T*>(&vz);
+#pragma unroll
+                for (int k = 0; k < VN; k++)
+                    p = fma(ax[k], ay[k] * az[k], p);
+            }
+        }
+        for (int o = G / 2; o > 0; o >>= 1)
+            p += __shfl_xor_sync(FULL, p, o);
+        if (act && gl == 0)
+            err[e] = tile_value<T>(q, a.val64, h.eoff + e) - p;
+    }
+    __syncthreads();
+    hook.after_errors();
+    // 3. owner segments: reduce in registers, one vector add per 16 bytes
+    //    (BF16 without a master: two bf16x2 adds per 4 elements)
+    for (int s0 = warp * EPW; s0 < h.nseg; s0 += seg_stride) {
+        const int s = s0 + sub;
+        const unsigned sg = sg_next;
+        if (s + seg_stride < h.nseg)
+            sg_next = __ldg(&a.segs[h.soff + s + seg_stride]);
+        if (s >= h.nseg)
+            continue;
+        const int row = seg_row(sg), m = seg_mode(sg), cnt = seg_count(sg);
+        const unsigned short* lst = csr + m * h.n + seg_start(sg);
+        T acc[E];
+#pragma unroll
+        for (int i = 0; i < E; i++)
+            acc[i] = T(0);
+        for (int k = 0; k < cnt; k++) {
+            const int e = lst[k];
+            const int4 q = ent[e];
+            const int l0 = q.x & 0xffff, l1 = (int)((unsigned)q.x >> 16), l2 = q.y;
+            const int o1 = m == 0 ? l1 : l0;
+            const int o2 = m == 2 ? l1 : l2;
+            const T er = err[e];
+            const size_t r1 = (size_t)o1 * Rp, r2 = (size_t)o2 * Rp;
+#pragma unroll
+            for (int j = 0; j < NV; j++) {
+                const int o = (j * G + gl) * VN;
+                if (MASK && o >= Rp)
+                    continue;
+                V v1, v2;
+                if constexpr (BF) {
+                    const unsigned short* Sb = reinterpret_cast<const unsigned short*>(smem);
+                    v1 = ld_bf4(Sb + r1 + o);
+                    v2 = ld_bf4(Sb + r2 + o);
+                } else {
+                    v1 = *reinterpret_cast<const V*>(S + r1 + o);
+                    v2 = *reinterpret_cast<const V*>(S + r2 + o);
+                }
+                const T* b1 = reinterpret_cast<const T*>(&v1);
+                const T* b2 = reinterpret_cast<const T*>(&v2);
+#pragma unroll
+                for (int i = 0; i < VN; i++)
+                    acc[j * VN + i] = fma(er, b1[i] * b2[i], acc[j * VN + i]);
+            }
+        }
+        const T* sr = S + (size_t)row * Rp;
+        const T w = m == 0 ? cx : (m == 1 ? cy : cz);
+        const T creg = (T)cnt * reg;
+        // Regularisation of a FAST row (one the host found decaying
+        // quickly relative to a tile's share of the epoch) takes the
+        // row's value at write time, not the tile-start snapshot: such
+        // a row is stepped by many concurrent tiles, and a decay
+        // computed from a value one tile old is delayed negative
+        // feedback whose gain grows with that concurrency until it
+        // diverges.  In BF16 every FAST row has a master.
+        if constexpr (BF) {
+            const int g = rid[row];  // global row, or ~(master index | FAST)
+            unsigned short* Fm = static_cast<unsigned short*>(m == 0 ? a.A : (m == 1 ? a.B : a.C));
+#pragma unroll
+            for (int j = 0; j < NV; j++) {
+                const int o = (j * G + gl) * VN;
+                if (MASK && o >= Rp)
+                    continue;
+                const float wc = w * creg;
+                const float4 wa = make_float4(w * acc[j * VN + 0], w * acc[j * VN + 1],
+                                              w * acc[j * VN + 2], w * acc[j * VN + 3]);
+                const uint2 raw = *reinterpret_cast<const uint2*>(
+                    reinterpret_cast<const unsigned short*>(smem) + (size_t)row * Rp + o);
+                if (g < 0) {
+                    float* mp = (m == 0 ? a.master[0] : (m == 1 ? a.master[1] : a.master[2])) +
+                                (size_t)(~g & (FAST - 1)) * Rp + o;
+                    const float4 base = (~g & FAST) ? __ldcg(reinterpret_cast<const float4*>(mp))
+                                                    : bf16x4_to_float4(raw);
+                    red_v(mp, make_float4(wa.x - wc * base.x, wa.y - wc * base.y, wa.z - wc * base.z,
+                                          wa.w - wc * base.w));
+                } else if (wa.x != 0.f || wa.y != 0.f || wa.z != 0.f || wa.w != 0.f || raw.x || raw.y) {
+                    // fresh random bits for every rounding: a row without a
+                    // master is written at most once per tile visit, and a
+                    // block padded into several slots visits its tiles once
+                    // per slot, so (epoch seed, mode, slot, tile, row,
+                    // column) names one update.  Bits reused across the
+                    // updates of an epoch would round an element the same
+                    // way every time and let its magnitude drift by up to
+                    // one ulp per update.
+                    // The new value is computed from the snapshot and rounded
+                    // stochastically; its difference to the snapshot (a few
+                    // ulps, exact in BF16) lands by fire-and-forget bf16x2
+                    // atomic adds, skipped when the rounding left the pair
+                    // unchanged.  With no other tile on the row since the
+                    // snapshot the result is exactly the rounded value.
+                    __nv_bfloat162* wp = reinterpret_cast<__nv_bfloat162*>(Fm + (size_t)g * Rp + o);
+                    const unsigned rnd0 =
+                        mix3(tile_bits ^ (unsigned)(m * 0x68E31DA4u), (unsigned)g, (unsigned)o);
+                    const unsigned rnd1 = fmix32(rnd0 ^ 0x5BD1E995u);
+                    const float4 own = bf16x4_to_float4(raw);
+                    const float n0 = __uint_as_float(sr_bf16_bits(sr_step(own.x, wa.x, wc), rnd0) << 16);
+                    const float n1 = __uint_as_float(sr_bf16_bits(sr_step(own.y, wa.y, wc), rnd0 >> 16) << 16);
+                    const float n2 = __uint_as_float(sr_bf16_bits(sr_step(own.z, wa.z, wc), rnd1) << 16);
+                    const float n3 = __uint_as_float(sr_bf16_bits(sr_step(own.w, wa.w, wc), rnd1 >> 16) << 16);
+                    if (n0 != own.x || n1 != own.y)
+                        atomicAdd(wp, __floats2bfloat162_rn(n0 - own.x, n1 - own.y));
+                    if (n2 != own.z || n3 != own.w)
+                        atomicAdd(wp + 1, __floats2bfloat162_rn(n2 - own.z, n3 - own.w));
+                }
+            }
+        } else {
+            const int v = rid[row];  // global row, or ~row (FAST)
+            T* gr = (m == 0 ? FA : (m == 1 ? FB : FC)) + (size_t)(v < 0 ? ~v : v) * Rp;
+#pragma unroll
+            for (int j = 0; j < NV; j++) {
+                const int o = (j * G + gl) * VN;
+                if (MASK && o >= Rp)
+                    continue;
+                V d;
+                T* dd = reinterpret_cast<T*>(&d);
+                if (v < 0) {
+                    const V cur = __ldcg(reinterpret_cast<const V*>(gr + o));
+                    const T* cc = reinterpret_cast<const T*>(&cur);
+#pragma unroll
+                    for (int i = 0; i < VN; i++)
+                        dd[i] = w * (acc[j * VN + i] - creg * cc[i]);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < VN; i++)
+                        dd[i] = w * (acc[j * VN + i] - creg * sr[o + i]);
+                }
+                red_v(gr + o, d);
+            }
+        }
+    }
+    // the slot's next tile must see these adds (nothing orders the
+    // adds of different slots, so the last tile needs no fence)
+    if (fence)
+        __threadfence();
+    __syncthreads();
+        if (a.tile_ns && tid == 0) {
+            unsigned long long t_end;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_end));
+            a.tile_ns[t] = (unsigned)min(t_end - t_start, 0xffffffffull);
+        }
+}
+
+// One work unit of one tensor: slots [unit_off[unit], unit_off[unit+1]),
+// tile by tile.
+template <typename T, int GC, int NV, bool BF, bool MASK>
+__device__ __forceinline__ void run_unit(const StagedArgs& a, int unit, unsigned char* smem)
+{
+    const StagedLayout L(BF ? 2 : sizeof(T), a.Rp, a.cap, a.wave);
+    int* rid = reinterpret_cast<int*>(smem + L.rid);
     const T* coe = static_cast<const T*>(a.slot_coe);
     const unsigned seed = a.seed_ptr ? (a.seed ^ *a.seed_ptr) : a.seed;
-    {
-        const int u0 = __ldg(&a.unit_off[unit]), u1 = __ldg(&a.unit_off[unit + 1]);
-      for (int slot = u0; slot < u1; slot++) {
+    const int u0 = __ldg(&a.unit_off[unit]), u1 = __ldg(&a.unit_off[unit + 1]);
+    for (int slot = u0; slot < u1; slot++) {
         const T cx = coe[3 * slot], cy = coe[3 * slot + 1], cz = coe[3 * slot + 2];
         const int t0 = __ldg(&a.slot_tile0[slot]);
         const int t1 = t0 + __ldg(&a.slot_ntiles[slot]);
         for (int t = t0; t < t1; t++) {
-            unsigned long long t_start = 0;
-            if (a.tile_ns && tid == 0)
-                asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
             const TileHdr h = a.tiles[t];
-            const int nv = h.nrows * vpr;
-            const int nxy = h.nx + h.ny;
-            // rounding stream of this visit of this tile (BF16)
-            const unsigned tile_bits = BF ? mix3(seed, (unsigned)t, (unsigned)slot) : 0u;
-            // the first owner segment of this lane group, fetched now so that
-            // its latency hides behind staging and the errors
-            const int seg_stride = nwarps * EPW;
-            unsigned sg_next = 0;
-            if (warp * EPW + sub < h.nseg)
-                sg_next = __ldg(&a.segs[h.soff + warp * EPW + sub]);
-            // 1. stage: rows, entries and CSR lists, all as 16-byte async copies
-            //    (BF16 rows are widened to FP32 through registers)
-            if constexpr (BF) {
-                const int cpr = Rp / 8;  // 16-byte chunks per BF16 row
-                const int nc = h.nrows * cpr;
-                unsigned short* Sb = reinterpret_cast<unsigned short*>(smem);
-                for (int i = tid; i < nc; i += blockDim.x) {
-                    const int r = i / cpr, c = i - r * cpr;
-                    // the global row, or ~(master index | FAST) for a row with an FP32 master
-                    const int g = __ldg(&a.rows[h.roff + r]);
-                    const int m = r < h.nx ? 0 : (r < nxy ? 1 : 2);
-                    if (c == 0)
-                        rid[r] = g;
-                    if (g < 0) {
-                        const float* mm = m == 0 ? a.master[0] : (m == 1 ? a.master[1] : a.master[2]);
-                        const size_t hm = (size_t)(~g & (FAST - 1));
-                        const float4 v0 = __ldcg(reinterpret_cast<const float4*>(mm + hm * Rp + c * 8));
-                        const float4 v1 = __ldcg(reinterpret_cast<const float4*>(mm + hm * Rp + c * 8 + 4));
-                        uint4 q;
-                        q.x = pack_bf16x2_rn(v0.x, v0.y);
-                        q.y = pack_bf16x2_rn(v0.z, v0.w);
-                        q.z = pack_bf16x2_rn(v1.x, v1.y);
-                        q.w = pack_bf16x2_rn(v1.z, v1.w);
-                        *reinterpret_cast<uint4*>(Sb + (size_t)r * Rp + c * 8) = q;
-                    } else {
-                        const unsigned short* Fm = static_cast<const unsigned short*>(
-                            m == 0 ? a.A : (m == 1 ? a.B : a.C));
-                        cp16(Sb + (size_t)r * Rp + c * 8, Fm + (size_t)g * Rp + c * 8);
-                    }
-                }
-            }
-            for (int i = tid; i < (BF ? 0 : nv); i += blockDim.x) {
-                const int r = i / vpr, c = i - r * vpr;
-                const int g0 = __ldg(&a.rows[h.roff + r]);  // the global row, or ~row (FAST)
-                const int g = g0 < 0 ? ~g0 : g0;
-                if constexpr (BF) {
-                    // rows stay BF16 in shared memory: 16-byte chunks of 8
-                    // elements, copied as they are; hot rows are rounded from
-                    // their FP32 masters
-                    (void)c;
-                }
-                if constexpr (!BF) {
-                    if (c == 0)
-                        rid[r] = g0;
-                    const T* Fm = r < h.nx ? FA : (r < nxy ? FB : FC);
-                    cp16(reinterpret_cast<V*>(S) + i, reinterpret_cast<const V*>(Fm + (size_t)g * Rp) + c);
-                }
-            }
-            for (int i = tid; i < h.n; i += blockDim.x)
-                cp16(ent + i, a.ent + h.eoff + i);
-            const int nc = (3 * h.n + 7) >> 3;
-            for (int i = tid; i < nc; i += blockDim.x)
-                cp16(csr + 8 * i, a.csr + h.coff + 8 * i);
-            cp_wait_all();
-            __syncthreads();
-            // 2. errors
-            for (int e0 = warp * EPW; e0 < h.n; e0 += nwarps * EPW) {
-                const int e = e0 + sub;
-                const bool act = e < h.n;
-                T p = T(0);
-                int4 q = make_int4(0, 0, 0, 0);
-                if (act) {
-                    q = ent[e];
-                    const size_t rx = (size_t)(q.x & 0xffff) * Rp, ry = (size_t)((unsigned)q.x >> 16) * Rp,
-                                 rz = (size_t)q.y * Rp;
-#pragma unroll
-                    for (int j = 0; j < NV; j++) {
-                        const int o = (j * G + gl) * VN;
-                        if (MASK && o >= Rp)
-                            continue;
-                        V vx, vy, vz;
-                        if constexpr (BF) {
-                            const unsigned short* Sb = reinterpret_cast<const unsigned short*>(smem);
-                            vx = ld_bf4(Sb + rx + o);
-                            vy = ld_bf4(Sb + ry + o);
-                            vz = ld_bf4(Sb + rz + o);
-                        } else {
-                            vx = *reinterpret_cast<const V*>(S + rx + o);
-                            vy = *reinterpret_cast<const V*>(S + ry + o);
-                            vz = *reinterpret_cast<const V*>(S + rz + o);
-                        }
-                        const T* ax = reinterpret_cast<const T*>(&vx);
-                        const T* ay = reinterpret_cast<const T*>(&vy);
-                        const T* az = reinterpret_cast<const T*>(&vz);
-#pragma unroll
-                        for (int k = 0; k < VN; k++)
-                            p = fma(ax[k], ay[k] * az[k], p);
-                    }
-                }
-                for (int o = G / 2; o > 0; o >>= 1)
-                    p += __shfl_xor_sync(FULL, p, o);
-                if (act && gl == 0)
-                    err[e] = tile_value<T>(q, a.val64, h.eoff + e) - p;
-            }
-            __syncthreads();
-            // 3. owner segments: reduce in registers, one vector add per 16 bytes
-            //    (BF16 without a master: two bf16x2 adds per 4 elements)
-            for (int s0 = warp * EPW; s0 < h.nseg; s0 += seg_stride) {
-                const int s = s0 + sub;
-                const unsigned sg = sg_next;
-                if (s + seg_stride < h.nseg)
-                    sg_next = __ldg(&a.segs[h.soff + s + seg_stride]);
-                if (s >= h.nseg)
-                    continue;
-                const int row = seg_row(sg), m = seg_mode(sg), cnt = seg_count(sg);
-                const unsigned short* lst = csr + m * h.n + seg_start(sg);
-                T acc[E];
-#pragma unroll
-                for (int i = 0; i < E; i++)
-                    acc[i] = T(0);
-                for (int k = 0; k < cnt; k++) {
-                    const int e = lst[k];
-                    const int4 q = ent[e];
-                    const int l0 = q.x & 0xffff, l1 = (int)((unsigned)q.x >> 16), l2 = q.y;
-                    const int o1 = m == 0 ? l1 : l0;
-                    const int o2 = m == 2 ? l1 : l2;
-                    const T er = err[e];
-                    const size_t r1 = (size_t)o1 * Rp, r2 = (size_t)o2 * Rp;
-#pragma unroll
-                    for (int j = 0; j < NV; j++) {
-                        const int o = (j * G + gl) * VN;
-                        if (MASK && o >= Rp)
-                            continue;
-                        V v1, v2;
-                        if constexpr (BF) {
-                            const unsigned short* Sb = reinterpret_cast<const unsigned short*>(smem);
-                            v1 = ld_bf4(Sb + r1 + o);
-                            v2 = ld_bf4(Sb + r2 + o);
-                        } else {
-                            v1 = *reinterpret_cast<const V*>(S + r1 + o);
-                            v2 = *reinterpret_cast<const V*>(S + r2 + o);
-                        }
-                        const T* b1 = reinterpret_cast<const T*>(&v1);
-                        const T* b2 = reinterpret_cast<const T*>(&v2);
-#pragma unroll
-                        for (int i = 0; i < VN; i++)
-                            acc[j * VN + i] = fma(er, b1[i] * b2[i], acc[j * VN + i]);
-                    }
-                }
-                const T* sr = S + (size_t)row * Rp;
-                const T w = m == 0 ? cx : (m == 1 ? cy : cz);
-                const T creg = (T)cnt * reg;
-                // Regularisation of a FAST row (one the host found decaying
-                // quickly relative to a tile's share of the epoch) takes the
-                // row's value at write time, not the tile-start snapshot: such
-                // a row is stepped by many concurrent tiles, and a decay
-                // computed from a value one tile old is delayed negative
-                // feedback whose gain grows with that concurrency until it
-                // diverges.  In BF16 every FAST row has a master.
-                if constexpr (BF) {
-                    const int g = rid[row];  // global row, or ~(master index | FAST)
-                    unsigned short* Fm = static_cast<unsigned short*>(m == 0 ? a.A : (m == 1 ? a.B : a.C));
-#pragma unroll
-                    for (int j = 0; j < NV; j++) {
-                        const int o = (j * G + gl) * VN;
-                        if (MASK && o >= Rp)
-                            continue;
-                        const float wc = w * creg;
-                        const float4 wa = make_float4(w * acc[j * VN + 0], w * acc[j * VN + 1],
-                                                      w * acc[j * VN + 2], w * acc[j * VN + 3]);
-                        const uint2 raw = *reinterpret_cast<const uint2*>(
-                            reinterpret_cast<const unsigned short*>(smem) + (size_t)row * Rp + o);
-                        if (g < 0) {
-                            float* mp = (m == 0 ? a.master[0] : (m == 1 ? a.master[1] : a.master[2])) +
-                                        (size_t)(~g & (FAST - 1)) * Rp + o;
-                            const float4 base = (~g & FAST) ? __ldcg(reinterpret_cast<const float4*>(mp))
-                                                            : bf16x4_to_float4(raw);
-                            red_v(mp, make_float4(wa.x - wc * base.x, wa.y - wc * base.y, wa.z - wc * base.z,
-                                                  wa.w - wc * base.w));
-                        } else if (wa.x != 0.f || wa.y != 0.f || wa.z != 0.f || wa.w != 0.f || raw.x || raw.y) {
-                            // fresh random bits for every rounding: a row without a
-                            // master is written at most once per tile visit, and a
-                            // block padded into several slots visits its tiles once
-                            // per slot, so (epoch seed, mode, slot, tile, row,
-                            // column) names one update.  Bits reused across the
-                            // updates of an epoch would round an element the same
-                            // way every time and let its magnitude drift by up to
-                            // one ulp per update.
-                            // The new value is computed from the snapshot and rounded
-                            // stochastically; its difference to the snapshot (a few
-                            // ulps, exact in BF16) lands by fire-and-forget bf16x2
-                            // atomic adds, skipped when the rounding left the pair
-                            // unchanged.  With no other tile on the row since the
-                            // snapshot the result is exactly the rounded value.
-                            __nv_bfloat162* wp = reinterpret_cast<__nv_bfloat162*>(Fm + (size_t)g * Rp + o);
-                            const unsigned rnd0 =
-                                mix3(tile_bits ^ (unsigned)(m * 0x68E31DA4u), (unsigned)g, (unsigned)o);
-                            const unsigned rnd1 = fmix32(rnd0 ^ 0x5BD1E995u);
-                            const float4 own = bf16x4_to_float4(raw);
-                            const float n0 = __uint_as_float(sr_bf16_bits(sr_step(own.x, wa.x, wc), rnd0) << 16);
-                            const float n1 = __uint_as_float(sr_bf16_bits(sr_step(own.y, wa.y, wc), rnd0 >> 16) << 16);
-                            const float n2 = __uint_as_float(sr_bf16_bits(sr_step(own.z, wa.z, wc), rnd1) << 16);
-                            const float n3 = __uint_as_float(sr_bf16_bits(sr_step(own.w, wa.w, wc), rnd1 >> 16) << 16);
-                            if (n0 != own.x || n1 != own.y)
-                                atomicAdd(wp, __floats2bfloat162_rn(n0 - own.x, n1 - own.y));
-                            if (n2 != own.z || n3 != own.w)
-                                atomicAdd(wp + 1, __floats2bfloat162_rn(n2 - own.z, n3 - own.w));
-                        }
-                    }
-                } else {
-                    const int v = rid[row];  // global row, or ~row (FAST)
-                    T* gr = (m == 0 ? FA : (m == 1 ? FB : FC)) + (size_t)(v < 0 ? ~v : v) * Rp;
-#pragma unroll
-                    for (int j = 0; j < NV; j++) {
-                        const int o = (j * G + gl) * VN;
-                        if (MASK && o >= Rp)
-                            continue;
-                        V d;
-                        T* dd = reinterpret_cast<T*>(&d);
-                        if (v < 0) {
-                            const V cur = __ldcg(reinterpret_cast<const V*>(gr + o));
-                            const T* cc = reinterpret_cast<const T*>(&cur);
-#pragma unroll
-                            for (int i = 0; i < VN; i++)
-                                dd[i] = w * (acc[j * VN + i] - creg * cc[i]);
-                        } else {
-#pragma unroll
-                            for (int i = 0; i < VN; i++)
-                                dd[i] = w * (acc[j * VN + i] - creg * sr[o + i]);
-                        }
-                        red_v(gr + o, d);
-                    }
-                }
-            }
-            // the slot's next tile must see these adds (nothing orders the
-            // adds of different slots, so the last tile needs no fence)
-            if (t + 1 < t1)
-                __threadfence();
-            __syncthreads();
-            if (a.tile_ns && tid == 0) {
-                unsigned long long t_end;
-                asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_end));
-                a.tile_ns[t] = (unsigned)min(t_end - t_start, 0xffffffffull);
-            }
+            do_tile<T, GC, NV, BF, MASK>(a, smem, h, t, slot, cx, cy, cz, rid, false, t + 1 < t1, seed, NoHook());
         }
-      }
     }
 }
 
+// A CTA's place in its stream of tiles: work unit, slot, tile, the slot's
+// tile end (tile < 0: the stream has ended).
+struct Pos {
+    int unit, slot, t, t_end;
+};
+
+// The first tile of work unit u (t = -1 when u is past the last unit).
+__device__ __forceinline__ Pos first_pos(const StagedArgs& a, int u)
+{
+    Pos p{u, 0, -1, -1};
+    if (u >= a.nunits)
+        return p;
+    p.slot = __ldg(&a.unit_off[u]);
+    p.t = __ldg(&a.slot_tile0[p.slot]);
+    p.t_end = p.t + __ldg(&a.slot_ntiles[p.slot]);
+    return p;
+}
+
+// The tile after p: the slot's next tile, else the unit's next slot, else
+// the first tile of the unit taken ahead (*ahead), replaced by a new one from
+// the counter.
+__device__ __forceinline__ Pos next_pos(const StagedArgs& a, Pos p, int* ahead)
+{
+    if (p.t + 1 < p.t_end) {
+        p.t++;
+        return p;
+    }
+    if (p.slot + 1 < __ldg(&a.unit_off[p.unit + 1])) {
+        p.slot++;
+        p.t = __ldg(&a.slot_tile0[p.slot]);
+        p.t_end = p.t + __ldg(&a.slot_ntiles[p.slot]);
+        return p;
+    }
+    const int u = *ahead;
+    if (u < a.nunits)
+        *ahead = atomicAdd(a.counter, 1);
+    return first_pos(a, u);
+}
+
+// Loads the next tile's header (after the current tile is staged) and its
+// staged row ids (after the current tile's errors), so that the next tile's
+// row copies start without waiting on either.
+struct Ahead {
+    const StagedArgs* a;
+    const Pos* pos;   // the next tile's position (shared)
+    TileHdr* hdr;     // its header slot (shared)
+    int* rid;         // its row-id buffer (shared)
+    __device__ __forceinline__ void after_stage() const
+    {
+        if (threadIdx.x < 4 && pos->t >= 0)
+            reinterpret_cast<int4*>(hdr)[threadIdx.x] = __ldg(reinterpret_cast<const int4*>(a->tiles + pos->t) +
+                                                              threadIdx.x);
+    }
+    __device__ __forceinline__ void after_errors() const
+    {
+        if (pos->t < 0)
+            return;
+        const int n = hdr->nrows;
+        const int* src = a->rows + hdr->roff;
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+            rid[i] = __ldg(src + i);
+    }
+};
+
+// The single-tensor kernel: every CTA walks its stream of tiles -- work
+// units taken from the counter one ahead, their slots, the slots' tiles --
+// and fetches each next tile's header and row ids while the current tile
+// computes (two buffers each in shared memory).
 template <typename T, int G, int NV, bool BF>
 __global__ void __launch_bounds__(256, 4) k_staged(StagedArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ int s_unit;
+    __shared__ Pos s_pos[2];
+    __shared__ int s_ahead;
+    const StagedLayout L(BF ? 2 : sizeof(T), a.Rp, a.cap, a.wave);
+    TileHdr* hdr = reinterpret_cast<TileHdr*>(smem + L.hdr);
+    int* const rid0 = reinterpret_cast<int*>(smem + L.rid);
+    int* const rid1 = reinterpret_cast<int*>(smem + L.rid2);
+    const T* coe = static_cast<const T*>(a.slot_coe);
+    const unsigned seed = a.seed_ptr ? (a.seed ^ *a.seed_ptr) : a.seed;
+    if (threadIdx.x == 0) {
+        const int u = atomicAdd(a.counter, 1);
+        s_ahead = atomicAdd(a.counter, 1);
+        s_pos[0] = first_pos(a, u);
+    }
+    __syncthreads();
+    if (s_pos[0].t < 0)
+        return;
+    // the first tile's header and row ids, fetched in place
+    if (threadIdx.x < 4)
+        reinterpret_cast<int4*>(hdr)[threadIdx.x] = __ldg(reinterpret_cast<const int4*>(a.tiles + s_pos[0].t) +
+                                                          threadIdx.x);
+    __syncthreads();
+    for (int i = threadIdx.x; i < hdr[0].nrows; i += blockDim.x)
+        rid0[i] = __ldg(a.rows + hdr[0].roff + i);
+    __syncthreads();
+    int cur = 0, cur_slot = -1;
+    T cx = T(0), cy = T(0), cz = T(0);
     for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0)
-            s_unit = atomicAdd(a.counter, 1);
-        __syncthreads();
-        const int unit = s_unit;
-        if (unit >= a.nunits)
+        const Pos p = s_pos[cur];
+        if (p.t < 0)
             break;
-        run_unit<T, G, NV, BF, false>(a, unit, smem);
+        const int nxt = cur ^ 1;
+        // published by the tile's first barrier, before any thread reads it
+        if (threadIdx.x == 0)
+            s_pos[nxt] = next_pos(a, p, &s_ahead);
+        if (p.slot != cur_slot) {
+            cx = coe[3 * p.slot];
+            cy = coe[3 * p.slot + 1];
+            cz = coe[3 * p.slot + 2];
+            cur_slot = p.slot;
+        }
+        const TileHdr h = hdr[cur];
+        const Ahead hook{&a, &s_pos[nxt], &hdr[nxt], nxt ? rid1 : rid0};
+        do_tile<T, G, NV, BF, false>(a, smem, h, p.t, p.slot, cx, cy, cz, cur ? rid1 : rid0, true, p.t + 1 < p.t_end,
+                                     seed, hook);
+        cur = nxt;
     }
 }
 

@@ -42,12 +42,13 @@ struct StagedArgs {
     const unsigned* seed_ptr;  // when set, the rounding stream is seed ^ *seed_ptr (graph replays)
 };
 
-// Shared-memory layout of one CTA: S rows | entries | errors | row ids | CSR.
-// Every region that receives 16-byte copies starts on a 16-byte boundary.
-// es = bytes of one staged row element (8 FP64, 4 FP32, 2 BF16); errors are
-// kept in the compute type (8 for FP64, else 4).
+// Shared-memory layout of one CTA: S rows | entries | errors | row ids (two
+// buffers: the current tile's and the next one's, fetched ahead) | two tile
+// headers | CSR.  Every region that receives 16-byte copies starts on a
+// 16-byte boundary.  es = bytes of one staged row element (8 FP64, 4 FP32,
+// 2 BF16); errors are kept in the compute type (8 for FP64, else 4).
 struct StagedLayout {
-    size_t ent, err, rid, csr, total;
+    size_t ent, err, rid, rid2, hdr, csr, total;
     __host__ __device__ StagedLayout(size_t es, int Rp, int cap, int wave)
     {
         auto al = [](size_t v) { return (v + 15) & ~(size_t)15; };
@@ -55,7 +56,9 @@ struct StagedLayout {
         ent = al((size_t)cap * Rp * es);
         err = al(ent + (size_t)wave * 16);
         rid = al(err + (size_t)wave * ee);
-        csr = al(rid + (size_t)cap * 4);
+        rid2 = al(rid + (size_t)cap * 4);
+        hdr = al(rid2 + (size_t)cap * 4);
+        csr = al(hdr + 2 * sizeof(TileHdr));
         total = al(csr + (3 * (size_t)wave + 8) * 2);
     }
 };
