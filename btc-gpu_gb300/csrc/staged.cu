@@ -638,7 +638,10 @@ size_t staged_smem_bytes(int dtype, int Rp, int cap, int wave)
 int staged_cap_for(int dtype, int Rp, int wave, int ctas_per_sm, size_t smem_per_sm, size_t smem_per_block)
 {
     size_t es = dtype == 1 ? 8 : (dtype == 2 ? 2 : 4);
-    size_t budget = std::min(smem_per_block, smem_per_sm / (size_t)std::max(1, ctas_per_sm) - 1024);
+    // per CTA the SM reserves 1 KB, and the kernels' static shared
+    // variables (work positions, <= 64 bytes) come on top of the dynamic
+    // layout: a layout that filled the rest would cost one resident CTA
+    size_t budget = std::min(smem_per_block - 128, smem_per_sm / (size_t)std::max(1, ctas_per_sm) - 1024 - 128);
     int cap = (int)std::min<size_t>(16383, budget / ((size_t)Rp * es + 4));
     while (cap > 0 && staged_smem_bytes(dtype, Rp, cap, wave) > budget)
         cap--;
