@@ -705,6 +705,28 @@ static btc_status ctx_build(btc_ctx* c, const btc::Schedule& s, const int32_t* t
             });
             if (bad_seg)
                 return BTC_ERR_UNSUPPORTED;
+            // Within a tile the segments are independent (each adds to its
+            // own row), and a warp reduces EPW of them side by side for as
+            // many steps as the longest has entries: a stable counting sort
+            // by count, longest first, gives each warp segments of about
+            // equal length.
+            parallel_for((int64_t)ts.tiles.size(), HT, [&](int64_t lo, int64_t hi) {
+                std::vector<uint32_t> tmp;
+                for (int64_t t = lo; t < hi; t++) {
+                    const btc::TileHdr& h = ts.tiles[(size_t)t];
+                    uint32_t* sg = seg32.data() + h.soff;
+                    tmp.assign(sg, sg + h.nseg);
+                    // key 15 - (count - 1): 0 for 16 entries; pos[key + 1]
+                    // counts, then the prefix sum makes pos[key] the start
+                    int pos[17] = {0};
+                    for (uint32_t w : tmp)
+                        pos[16 - (int)((w >> 16) & 15)]++;
+                    for (int k = 1; k <= 16; k++)
+                        pos[k] += pos[k - 1];
+                    for (uint32_t w : tmp)
+                        sg[pos[15 - (int)((w >> 16) & 15)]++] = w;
+                }
+            }, 1024);
             if ((rc = upload((void**)&c->tsegs, seg32.data(), seg32.size() * 4, c->stream)))
                 return rc;
         }

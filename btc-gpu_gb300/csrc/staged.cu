@@ -190,7 +190,8 @@ __device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem
     if (warp * EPW + sub < h.nseg)
         sg_next = __ldg(&a.segs[h.soff + warp * EPW + sub]);
     // 1. stage: rows, entries and CSR lists, all as 16-byte async copies
-    //    (BF16 rows are widened to FP32 through registers)
+    //    (BF16 rows stay BF16; a row with an FP32 master is rounded from it
+    //    through registers)
     if constexpr (BF) {
         const int cpr = Rp / 8;  // 16-byte chunks per BF16 row
         const int nc = h.nrows * cpr;
@@ -225,12 +226,6 @@ __device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem
         const int r = i / vpr, c = i - r * vpr;
         const int g0 = rid_ready ? rid[r] : __ldg(&a.rows[h.roff + r]);  // the global row, or ~row (FAST)
         const int g = g0 < 0 ? ~g0 : g0;
-        if constexpr (BF) {
-            // rows stay BF16 in shared memory: 16-byte chunks of 8
-            // elements, copied as they are; hot rows are rounded from
-            // their FP32 masters
-            (void)c;
-        }
         if constexpr (!BF) {
             if (!rid_ready && c == 0)
                 rid[r] = g0;
