@@ -74,7 +74,10 @@ __device__ __forceinline__ double tile_value<double>(const int4&, const double* 
 // uniform random bits below the truncation point and truncating (Gupta et
 // al., "Deep Learning with Limited Numerical Precision", 2015): the rounded
 // value is unbiased, so updates far below one BF16 ulp still move a row on
-// average.
+// average.  sm_100-family GPUs do it in one instruction per pair,
+// cvt.rs.bf16x2.f32 (PTX ISA 8.7): the high half rounds with rbits[31:16],
+// the low half with rbits[15:0], up when the 16 discarded mantissa bits plus
+// the random bits carry.
 __device__ __forceinline__ unsigned mix3(unsigned a, unsigned b, unsigned c)
 {
     unsigned h = a * 0x9E3779B1u ^ b * 0x85EBCA77u ^ c * 0xC2B2AE3Du;
@@ -85,23 +88,27 @@ __device__ __forceinline__ unsigned mix3(unsigned a, unsigned b, unsigned c)
     h ^= h >> 15;
     return h;
 }
-// The 32-bit finaliser of MurmurHash3 (Appleby): a bijection with full
-// avalanche, used to draw a second word of rounding bits from the first.
-__device__ __forceinline__ unsigned fmix32(unsigned h)
+// Word k of rounding bits drawn from a lane's hash h (full avalanche over
+// its inputs): a multiply by a distinct odd constant per k, and an
+// xor-shift that folds the product's well-mixed high half into its low half.
+__device__ __forceinline__ unsigned draw_bits(unsigned h, unsigned k)
 {
-    h ^= h >> 16;
-    h *= 0x85EBCA6Bu;
-    h ^= h >> 13;
-    h *= 0xC2B2AE35u;
-    h ^= h >> 16;
-    return h;
+    const unsigned w = h * (0x9E3779B1u + 0x3C6EF372u * k);
+    return w ^ (w >> 16);
 }
-__device__ __forceinline__ unsigned sr_bf16_bits(float x, unsigned r16)
+// {hi, lo} rounded stochastically to a bf16x2 word (hi in bits 31:16)
+__device__ __forceinline__ unsigned cvt_rs_bf16x2(float hi, float lo, unsigned rbits)
 {
-    unsigned u = __float_as_uint(x);
-    if ((u & 0x7f800000u) == 0x7f800000u)
-        return u >> 16;
-    return (u + (r16 & 0xffffu)) >> 16;
+    unsigned d;
+    asm("cvt.rs.satfinite.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
+    return d;
+}
+// Adds a - b (bf16x2, rounded to nearest) to the pair at p, fire and forget.
+__device__ __forceinline__ void red_bf16x2_diff(void* p, unsigned a, unsigned b)
+{
+    unsigned d;
+    asm("sub.rn.bf16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    asm volatile("red.global.add.noftz.bf16x2 [%0], %1;" ::"l"(p), "r"(d) : "memory");
 }
 __device__ __forceinline__ float4 bf16x4_to_float4(uint2 raw)
 {
@@ -339,6 +346,14 @@ __device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem
         if constexpr (BF) {
             const int g = rid[row];  // global row, or ~(master index | FAST)
             unsigned short* Fm = static_cast<unsigned short*>(m == 0 ? a.A : (m == 1 ? a.B : a.C));
+            // fresh random bits for every rounding: a row without a master
+            // is written at most once per tile visit, and a block padded
+            // into several slots visits its tiles once per slot, so (epoch
+            // seed, mode, slot, tile, row, lane, vector) names one update.
+            // Bits reused across the updates of an epoch would round an
+            // element the same way every time and let its magnitude drift by
+            // up to one ulp per update.
+            const unsigned hl = g >= 0 ? mix3(tile_bits ^ (unsigned)(m * 0x68E31DA4u), (unsigned)g, (unsigned)gl) : 0u;
 #pragma unroll
             for (int j = 0; j < NV; j++) {
                 const int o = (j * G + gl) * VN;
@@ -357,33 +372,22 @@ __device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem
                     red_v(mp, make_float4(wa.x - wc * base.x, wa.y - wc * base.y, wa.z - wc * base.z,
                                           wa.w - wc * base.w));
                 } else if (wa.x != 0.f || wa.y != 0.f || wa.z != 0.f || wa.w != 0.f || raw.x || raw.y) {
-                    // fresh random bits for every rounding: a row without a
-                    // master is written at most once per tile visit, and a
-                    // block padded into several slots visits its tiles once
-                    // per slot, so (epoch seed, mode, slot, tile, row,
-                    // column) names one update.  Bits reused across the
-                    // updates of an epoch would round an element the same
-                    // way every time and let its magnitude drift by up to
-                    // one ulp per update.
                     // The new value is computed from the snapshot and rounded
                     // stochastically; its difference to the snapshot (a few
                     // ulps, exact in BF16) lands by fire-and-forget bf16x2
                     // atomic adds, skipped when the rounding left the pair
                     // unchanged.  With no other tile on the row since the
                     // snapshot the result is exactly the rounded value.
-                    __nv_bfloat162* wp = reinterpret_cast<__nv_bfloat162*>(Fm + (size_t)g * Rp + o);
-                    const unsigned rnd0 =
-                        mix3(tile_bits ^ (unsigned)(m * 0x68E31DA4u), (unsigned)g, (unsigned)o);
-                    const unsigned rnd1 = fmix32(rnd0 ^ 0x5BD1E995u);
+                    unsigned short* wp = Fm + (size_t)g * Rp + o;
                     const float4 own = bf16x4_to_float4(raw);
-                    const float n0 = __uint_as_float(sr_bf16_bits(sr_step(own.x, wa.x, wc), rnd0) << 16);
-                    const float n1 = __uint_as_float(sr_bf16_bits(sr_step(own.y, wa.y, wc), rnd0 >> 16) << 16);
-                    const float n2 = __uint_as_float(sr_bf16_bits(sr_step(own.z, wa.z, wc), rnd1) << 16);
-                    const float n3 = __uint_as_float(sr_bf16_bits(sr_step(own.w, wa.w, wc), rnd1 >> 16) << 16);
-                    if (n0 != own.x || n1 != own.y)
-                        atomicAdd(wp, __floats2bfloat162_rn(n0 - own.x, n1 - own.y));
-                    if (n2 != own.z || n3 != own.w)
-                        atomicAdd(wp + 1, __floats2bfloat162_rn(n2 - own.z, n3 - own.w));
+                    const unsigned n01 = cvt_rs_bf16x2(sr_step(own.y, wa.y, wc), sr_step(own.x, wa.x, wc),
+                                                       draw_bits(hl, 2u * j));
+                    const unsigned n23 = cvt_rs_bf16x2(sr_step(own.w, wa.w, wc), sr_step(own.z, wa.z, wc),
+                                                       draw_bits(hl, 2u * j + 1u));
+                    if (n01 != raw.x)
+                        red_bf16x2_diff(wp, n01, raw.x);
+                    if (n23 != raw.y)
+                        red_bf16x2_diff(wp + 2, n23, raw.y);
                 }
             }
         } else {
