@@ -50,7 +50,13 @@ struct SV<double> {
     using V = double2;
 };
 
-__device__ __forceinline__ void red_v(float* p, float4 d) { atomicAdd(reinterpret_cast<float4*>(p), d); }
+// Vector adds to global memory that return nothing (red, not atom): no
+// register waits on the old value.
+__device__ __forceinline__ void red_v(float* p, float4 d)
+{
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(d.x), "f"(d.y), "f"(d.z), "f"(d.w)
+                 : "memory");
+}
 __device__ __forceinline__ void red_v(double* p, double2 d)
 {
     atomicAdd(p, d.x);
