@@ -77,9 +77,13 @@ __device__ __forceinline__ void ldrow_ro(const unsigned short* p, float* r)
     r[2] = __uint_as_float(v.y << 16);
     r[3] = __uint_as_float(v.y & 0xffff0000u);
 }
+// a vector add that returns nothing (red, not atom): no register waits on
+// the old value
 __device__ __forceinline__ void addrow(float* p, const float* d)
 {
-    atomicAdd(reinterpret_cast<float4*>(p), make_float4(d[0], d[1], d[2], d[3]));
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(d[0]), "f"(d[1]), "f"(d[2]),
+                 "f"(d[3])
+                 : "memory");
 }
 __device__ __forceinline__ void addrow(double* p, const double* d)
 {
