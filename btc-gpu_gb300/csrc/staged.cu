@@ -227,11 +227,11 @@ __device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem
                 q.y = pack_bf16x2_rn(v0.z, v0.w);
                 q.z = pack_bf16x2_rn(v1.x, v1.y);
                 q.w = pack_bf16x2_rn(v1.z, v1.w);
-                *reinterpret_cast<uint4*>(Sb + (size_t)r * Rp + c * 8) = q;
+                *reinterpret_cast<uint4*>(Sb + (r * Rp + c * 8)) = q;
             } else {
                 const unsigned short* Fm = static_cast<const unsigned short*>(
                     m == 0 ? a.A : (m == 1 ? a.B : a.C));
-                cp16(Sb + (size_t)r * Rp + c * 8, Fm + (size_t)g * Rp + c * 8);
+                cp16(Sb + (r * Rp + c * 8), Fm + (size_t)g * Rp + c * 8);
             }
         }
     }
@@ -262,8 +262,8 @@ __device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem
         int4 q = make_int4(0, 0, 0, 0);
         if (act) {
             q = ent[e];
-            const size_t rx = (size_t)(q.x & 0xffff) * Rp, ry = (size_t)((unsigned)q.x >> 16) * Rp,
-                         rz = (size_t)q.y * Rp;
+            // shared-memory offsets in 32-bit arithmetic
+            const int rx = (q.x & 0xffff) * Rp, ry = (int)((unsigned)q.x >> 16) * Rp, rz = q.y * Rp;
 #pragma unroll
             for (int j = 0; j < NV; j++) {
                 const int o = (j * G + gl) * VN;
@@ -272,13 +272,13 @@ __device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem
                 V vx, vy, vz;
                 if constexpr (BF) {
                     const unsigned short* Sb = reinterpret_cast<const unsigned short*>(smem);
-                    vx = ld_bf4(Sb + rx + o);
-                    vy = ld_bf4(Sb + ry + o);
-                    vz = ld_bf4(Sb + rz + o);
+                    vx = ld_bf4(Sb + (rx + o));
+                    vy = ld_bf4(Sb + (ry + o));
+                    vz = ld_bf4(Sb + (rz + o));
                 } else {
-                    vx = *reinterpret_cast<const V*>(S + rx + o);
-                    vy = *reinterpret_cast<const V*>(S + ry + o);
-                    vz = *reinterpret_cast<const V*>(S + rz + o);
+                    vx = *reinterpret_cast<const V*>(S + (rx + o));
+                    vy = *reinterpret_cast<const V*>(S + (ry + o));
+                    vz = *reinterpret_cast<const V*>(S + (rz + o));
                 }
                 const T* ax = reinterpret_cast<const T*>(&vx);
                 const T* ay = reinterpret_cast<const T*>(&vy);
@@ -317,7 +317,7 @@ __device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem
             const int o1 = m == 0 ? l1 : l0;
             const int o2 = m == 2 ? l1 : l2;
             const T er = err[e];
-            const size_t r1 = (size_t)o1 * Rp, r2 = (size_t)o2 * Rp;
+            const int r1 = o1 * Rp, r2 = o2 * Rp;
 #pragma unroll
             for (int j = 0; j < NV; j++) {
                 const int o = (j * G + gl) * VN;
@@ -326,11 +326,11 @@ __device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem
                 V v1, v2;
                 if constexpr (BF) {
                     const unsigned short* Sb = reinterpret_cast<const unsigned short*>(smem);
-                    v1 = ld_bf4(Sb + r1 + o);
-                    v2 = ld_bf4(Sb + r2 + o);
+                    v1 = ld_bf4(Sb + (r1 + o));
+                    v2 = ld_bf4(Sb + (r2 + o));
                 } else {
-                    v1 = *reinterpret_cast<const V*>(S + r1 + o);
-                    v2 = *reinterpret_cast<const V*>(S + r2 + o);
+                    v1 = *reinterpret_cast<const V*>(S + (r1 + o));
+                    v2 = *reinterpret_cast<const V*>(S + (r2 + o));
                 }
                 const T* b1 = reinterpret_cast<const T*>(&v1);
                 const T* b2 = reinterpret_cast<const T*>(&v2);
@@ -339,7 +339,7 @@ __device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem
                     acc[j * VN + i] = fma(er, b1[i] * b2[i], acc[j * VN + i]);
             }
         }
-        const T* sr = S + (size_t)row * Rp;
+        const T* sr = S + row * Rp;
         const T w = m == 0 ? cx : (m == 1 ? cy : cz);
         const T creg = (T)cnt * reg;
         // Regularisation of a FAST row (one the host found decaying
@@ -369,7 +369,7 @@ __device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem
                 const float4 wa = make_float4(w * acc[j * VN + 0], w * acc[j * VN + 1],
                                               w * acc[j * VN + 2], w * acc[j * VN + 3]);
                 const uint2 raw = *reinterpret_cast<const uint2*>(
-                    reinterpret_cast<const unsigned short*>(smem) + (size_t)row * Rp + o);
+                    reinterpret_cast<const unsigned short*>(smem) + (row * Rp + o));
                 if (g < 0) {
                     float* mp = (m == 0 ? a.master[0] : (m == 1 ? a.master[1] : a.master[2])) +
                                 (size_t)(~g & (FAST - 1)) * Rp + o;
