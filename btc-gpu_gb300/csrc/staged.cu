@@ -109,12 +109,17 @@ __device__ __forceinline__ unsigned cvt_rs_bf16x2(float hi, float lo, unsigned r
     asm("cvt.rs.satfinite.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
     return d;
 }
-// Adds a - b (bf16x2, rounded to nearest) to the pair at p, fire and forget.
+// Adds a - b (bf16x2, rounded to nearest) to the pair at p, fire and
+// forget, unless a == b: one predicated red, no branch.
 __device__ __forceinline__ void red_bf16x2_diff(void* p, unsigned a, unsigned b)
 {
-    unsigned d;
-    asm("sub.rn.bf16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
-    asm volatile("red.global.add.noftz.bf16x2 [%0], %1;" ::"l"(p), "r"(d) : "memory");
+    asm volatile(
+        "{\n\t.reg .pred q;\n\t.reg .b32 d;\n\t"
+        "setp.ne.b32 q, %1, %2;\n\t"
+        "sub.rn.bf16x2 d, %1, %2;\n\t"
+        "@q red.global.add.noftz.bf16x2 [%0], d;\n\t}" ::"l"(p),
+        "r"(a), "r"(b)
+        : "memory");
 }
 __device__ __forceinline__ float4 bf16x4_to_float4(uint2 raw)
 {
@@ -189,6 +194,12 @@ __device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem
     T* const FC = static_cast<T*>(a.C);
     const T reg = (T)a.reg;
     const int vpr = Rp / VN;
+    // 16-byte chunks per staged row (BF16 cpr, else vpr) and their log2 when
+    // a power of two (-1 otherwise): the staging loops split a chunk index
+    // into row and chunk by a shift instead of a division
+    const int cpr = Rp / 8;
+    const int cps = (cpr & (cpr - 1)) == 0 ? __ffs(cpr) - 1 : -1;
+    const int vps = (vpr & (vpr - 1)) == 0 ? __ffs(vpr) - 1 : -1;
     unsigned long long t_start = 0;
     if (a.tile_ns && tid == 0)
         asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
@@ -206,11 +217,10 @@ __device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem
     //    (BF16 rows stay BF16; a row with an FP32 master is rounded from it
     //    through registers)
     if constexpr (BF) {
-        const int cpr = Rp / 8;  // 16-byte chunks per BF16 row
         const int nc = h.nrows * cpr;
         unsigned short* Sb = reinterpret_cast<unsigned short*>(smem);
         for (int i = tid; i < nc; i += blockDim.x) {
-            const int r = i / cpr, c = i - r * cpr;
+            const int r = cps >= 0 ? i >> cps : i / cpr, c = i - r * cpr;
             // the global row, or ~(master index | FAST) for a row with an FP32 master
             // (from shared memory when the caller prefetched it)
             const int g = rid_ready ? rid[r] : __ldg(&a.rows[h.roff + r]);
@@ -236,7 +246,7 @@ __device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem
         }
     }
     for (int i = tid; i < (BF ? 0 : nv); i += blockDim.x) {
-        const int r = i / vpr, c = i - r * vpr;
+        const int r = vps >= 0 ? i >> vps : i / vpr, c = i - r * vpr;
         const int g0 = rid_ready ? rid[r] : __ldg(&a.rows[h.roff + r]);  // the global row, or ~row (FAST)
         const int g = g0 < 0 ? ~g0 : g0;
         if constexpr (!BF) {
@@ -377,23 +387,22 @@ __device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem
                                                     : bf16x4_to_float4(raw);
                     red_v(mp, make_float4(wa.x - wc * base.x, wa.y - wc * base.y, wa.z - wc * base.z,
                                           wa.w - wc * base.w));
-                } else if (wa.x != 0.f || wa.y != 0.f || wa.z != 0.f || wa.w != 0.f || raw.x || raw.y) {
+                } else {
                     // The new value is computed from the snapshot and rounded
                     // stochastically; its difference to the snapshot (a few
                     // ulps, exact in BF16) lands by fire-and-forget bf16x2
                     // atomic adds, skipped when the rounding left the pair
-                    // unchanged.  With no other tile on the row since the
-                    // snapshot the result is exactly the rounded value.
+                    // unchanged (always so for a zero step on a zero row).
+                    // With no other tile on the row since the snapshot the
+                    // result is exactly the rounded value.
                     unsigned short* wp = Fm + (size_t)g * Rp + o;
                     const float4 own = bf16x4_to_float4(raw);
                     const unsigned n01 = cvt_rs_bf16x2(sr_step(own.y, wa.y, wc), sr_step(own.x, wa.x, wc),
                                                        draw_bits(hl, 2u * j));
                     const unsigned n23 = cvt_rs_bf16x2(sr_step(own.w, wa.w, wc), sr_step(own.z, wa.z, wc),
                                                        draw_bits(hl, 2u * j + 1u));
-                    if (n01 != raw.x)
-                        red_bf16x2_diff(wp, n01, raw.x);
-                    if (n23 != raw.y)
-                        red_bf16x2_diff(wp + 2, n23, raw.y);
+                    red_bf16x2_diff(wp, n01, raw.x);
+                    red_bf16x2_diff(wp + 2, n23, raw.y);
                 }
             }
         } else {
