@@ -320,6 +320,7 @@ __device__ __forceinline__ void do_tile(const StagedArgs& a, unsigned char* smem
 #pragma unroll
         for (int i = 0; i < E; i++)
             acc[i] = T(0);
+#pragma unroll 2
         for (int k = 0; k < cnt; k++) {
             const int e = lst[k];
             const int4 q = ent[e];
