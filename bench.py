@@ -81,6 +81,10 @@ WORKLOADS = {
                 train=0.9, R=32, lr=0.005, reg=0.02, epochs=20,
                 desc="profiling case of the C2 shape: I=J=100k K=10k, 10M nnz Zipf(1.2) per mode, rank-16 GT + "
                      "N(0,0.05), 90/10 split, R=32, lr 0.005, lambda 0.02"),
+    "c5s": dict(I=1_000_000, J=1_000_000, K=100_000, nnz=200_000_000, zipf=(1.3, 1.3, 1.3), gt_rank=32,
+                noise=0.05, train=0.95, R=32, lr=0.005, reg=0.02, epochs=10,
+                desc="profiling case of the C5 shape: I=J=1M K=100k, 200M nnz Zipf(1.3) per mode, rank-32 GT + "
+                     "N(0,0.05), 95/5 split, R=32, lr 0.005, lambda 0.02"),
     "small": dict(I=20000, J=20000, K=5000, nnz=2_000_000, zipf=(1.2, 1.2, 1.2), gt_rank=16, noise=0.05,
                   train=0.9, R=32, lr=0.005, reg=0.02, epochs=10,
                   desc="small skewed: I=J=20k K=5k, 2M nnz Zipf(1.2), R=32"),
@@ -94,6 +98,7 @@ LEARN = dict(lr=0.005, reg=0.0005)
 TRAJ_EPOCHS = {"c5": (8, 30), "c3": (10, 40), "c2": (20, 60), "c1": (10, 60), "small": (10, 60)}
 SEED = 20261203 + 1
 CTAS = 0
+ROW_REPEAT = 0
 # DRAM bytes per launch of the timed kernel from an ncu capture of the same
 # workload (profiles/), keyed by (workload, dtype, mode); absent = null
 TRAFFIC = {("c2", "f32", "staged"): 1.556e9, ("c2", "f32", "hogwild"): 0.7786e9, ("c2", "bf16", "staged"): 1.366e9}
@@ -185,7 +190,8 @@ def cfg_for(w, dtype, mode, device=0):
     import btc_gpu as bg
 
     return bg.config(I=w["I"], J=w["J"], K=w["K"], rank=w["R"], lr=w["lr"], reg=w["reg"], block_s=2048,
-                     parallel_sequence_size=8, dtype=dtype, mode=mode, device=device, ctas_per_sm=CTAS)
+                     parallel_sequence_size=8, dtype=dtype, mode=mode, device=device, ctas_per_sm=CTAS,
+                     row_repeat=ROW_REPEAT)
 
 
 class Phases:
@@ -781,6 +787,8 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=60.0,
                     help="host-core time the reference arm spreads over its warm-up and timed steps")
     ap.add_argument("--ctas", type=int, default=0, help="staged kernel CTAs per SM (0 = auto)")
+    ap.add_argument("--row-repeat", type=int, default=0,
+                    help="staged tiles: most entries of one row per tile (0 = the library default)")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner and the learned work units")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned blocking")
@@ -788,8 +796,9 @@ def main():
     ap.add_argument("--traj-epochs", type=int, nargs=2, default=None,
                     help="epochs of the configured-regime and learning-regime trajectories")
     args = ap.parse_args()
-    global CTAS
+    global CTAS, ROW_REPEAT
     CTAS = args.ctas
+    ROW_REPEAT = args.row_repeat
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     if args.impl == "reference":

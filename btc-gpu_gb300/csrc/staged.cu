@@ -470,37 +470,47 @@ struct Pos {
     int unit, slot, t, t_end;
 };
 
-// The first tile of work unit u (t = -1 when u is past the last unit).
-__device__ __forceinline__ Pos first_pos(const StagedArgs& a, int u)
+// The first tile of unit u at or after slot `slot`, skipping slots whose
+// block has no entries (no tiles); t = -1 when the unit has none left.
+__device__ __forceinline__ Pos slot_pos(const StagedArgs& a, int u, int slot)
 {
-    Pos p{u, 0, -1, -1};
-    if (u >= a.nunits)
-        return p;
-    p.slot = __ldg(&a.unit_off[u]);
-    p.t = __ldg(&a.slot_tile0[p.slot]);
-    p.t_end = p.t + __ldg(&a.slot_ntiles[p.slot]);
-    return p;
+    const int s1 = __ldg(&a.unit_off[u + 1]);
+    for (; slot < s1; slot++) {
+        const int n = __ldg(&a.slot_ntiles[slot]);
+        if (n > 0) {
+            const int t = __ldg(&a.slot_tile0[slot]);
+            return Pos{u, slot, t, t + n};
+        }
+    }
+    return Pos{u, s1, -1, -1};
 }
 
-// The tile after p: the slot's next tile, else the unit's next slot, else
-// the first tile of the unit taken ahead (*ahead), replaced by a new one from
-// the counter.
+// The first tile of the unit taken ahead (*ahead), which is replaced by a new
+// one from the counter; units without tiles are passed over.  t = -1 once the
+// units are exhausted.
+__device__ __forceinline__ Pos unit_pos(const StagedArgs& a, int* ahead)
+{
+    for (;;) {
+        const int u = *ahead;
+        if (u >= a.nunits)
+            return Pos{u, 0, -1, -1};
+        *ahead = atomicAdd(a.counter, 1);
+        const Pos p = slot_pos(a, u, __ldg(&a.unit_off[u]));
+        if (p.t >= 0)
+            return p;
+    }
+}
+
+// The tile after p: the slot's next tile, else the first tile of the unit's
+// next slot that has tiles, else the first tile of the next unit.
 __device__ __forceinline__ Pos next_pos(const StagedArgs& a, Pos p, int* ahead)
 {
     if (p.t + 1 < p.t_end) {
         p.t++;
         return p;
     }
-    if (p.slot + 1 < __ldg(&a.unit_off[p.unit + 1])) {
-        p.slot++;
-        p.t = __ldg(&a.slot_tile0[p.slot]);
-        p.t_end = p.t + __ldg(&a.slot_ntiles[p.slot]);
-        return p;
-    }
-    const int u = *ahead;
-    if (u < a.nunits)
-        *ahead = atomicAdd(a.counter, 1);
-    return first_pos(a, u);
+    const Pos q = slot_pos(a, p.unit, p.slot + 1);
+    return q.t >= 0 ? q : unit_pos(a, ahead);
 }
 
 // Loads the next tile's header (after the current tile is staged) and its
@@ -545,9 +555,8 @@ __global__ void __launch_bounds__(256, 4) k_staged(StagedArgs a)
     const T* coe = static_cast<const T*>(a.slot_coe);
     const unsigned seed = a.seed_ptr ? (a.seed ^ *a.seed_ptr) : a.seed;
     if (threadIdx.x == 0) {
-        const int u = atomicAdd(a.counter, 1);
         s_ahead = atomicAdd(a.counter, 1);
-        s_pos[0] = first_pos(a, u);
+        s_pos[0] = unit_pos(a, &s_ahead);
     }
     __syncthreads();
     if (s_pos[0].t < 0)

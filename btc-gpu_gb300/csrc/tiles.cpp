@@ -197,7 +197,8 @@ void build_tiles(const Schedule& s, const int32_t* xyz, const double* val, int I
         for (int u = 0; u < t; u++)
             tile_base += (int)part[(size_t)u].tiles.size();
         for (size_t i = cut[(size_t)t]; i < cut[(size_t)t + 1]; i++) {
-            out.block_tile0[(size_t)order[i]] = tile_base + first[i];
+            // a block without entries has no tiles and no first tile
+            out.block_tile0[(size_t)order[i]] = count[i] > 0 ? tile_base + first[i] : -1;
             out.block_ntiles[(size_t)order[i]] = count[i];
         }
         out.max_rows = std::max(out.max_rows, part[(size_t)t].max_rows);

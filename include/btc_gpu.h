@@ -99,7 +99,7 @@ typedef struct btc_config {
     int32_t host_threads;           /* builder threads, 0 = hardware concurrency */
     int32_t ctas_per_sm;            /* staged kernel: CTAs sharing one SM's shared memory, 0 = auto */
     int32_t row_repeat;             /* staged kernel: most entries of one row in a tile; 0 = the
-                                       power of two at or below 0.32 / lr, in [16, 512] */
+                                       power of two at or below 0.16 / lr, in [16, 512] */
     int32_t reserved[5];
 } btc_config;
 
@@ -228,7 +228,8 @@ btc_status btc_eval(btc_ctx *ctx, int32_t split, btc_metrics *out);
 btc_status btc_ctx_tile_count(btc_ctx *ctx, int64_t *n);
 btc_status btc_ctx_tile_features(btc_ctx *ctx, float *features);
 btc_status btc_train_epoch_profiled(btc_ctx *ctx, uint32_t *tile_ns, btc_epoch_stats *stats);
-/* The tiles of each scheduled slot: tile0[slot], ntiles[slot] (num_slots each). */
+/* The tiles of each scheduled slot: tile0[slot], ntiles[slot] (num_slots each;
+   a slot whose block has no entries has tile0 -1 and ntiles 0). */
 btc_status btc_ctx_slot_tiles(btc_ctx *ctx, int32_t *tile0, int32_t *ntiles);
 /* Work units of the staged kernel: a CTA takes slots [unit_off[u],
  * unit_off[u+1]) at once (schedule order is kept).  unit_off[0] = 0,
