@@ -47,6 +47,7 @@ between strata); --gpus N under torchrun runs N independent replicas
 """
 import argparse
 import json
+import math
 import os
 import resource
 import statistics
@@ -102,6 +103,17 @@ ROW_REPEAT = 0
 # DRAM bytes per launch of the timed kernel from an ncu capture of the same
 # workload (profiles/), keyed by (workload, dtype, mode); absent = null
 TRAFFIC = {("c2", "f32", "staged"): 1.556e9, ("c2", "f32", "hogwild"): 0.7786e9, ("c2", "bf16", "staged"): 1.366e9}
+
+
+def finite(x):
+    """The line with every non-finite float as null (strict JSON has no NaN)."""
+    if isinstance(x, float):
+        return x if math.isfinite(x) else None
+    if isinstance(x, dict):
+        return {k: finite(v) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [finite(v) for v in x]
+    return x
 
 
 def log(*a):
@@ -296,7 +308,7 @@ def run_reference(args):
             "cpu_baseline": {"value": value, "unit": "updates/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+    print(json.dumps(finite(line)), flush=True)
     return 0
 
 
@@ -639,7 +651,7 @@ def run_gpu(args):
             line["oracle_check"] = check
         if clk:
             line["clocks"] = clk
-        print(json.dumps(line), flush=True)
+        print(json.dumps(finite(line)), flush=True)
     if model is not None:
         model.close()
     if dist:
@@ -770,7 +782,7 @@ def run_c4(args):
             "time_to_rmse": {"epochs": epochs_cmp, "tensors_reaching_target": len(reached),
                              "batched_bf16_ms_all_tensors": max((p["batched_bf16_ms"] for p in reached), default=None),
                              "plain_ms_sum_over_tensors": seq_total, "per_tensor": per}}
-    print(json.dumps(line), flush=True)
+    print(json.dumps(finite(line)), flush=True)
     return 0
 
 
