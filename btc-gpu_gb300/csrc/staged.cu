@@ -1,20 +1,25 @@
 // k_staged: the shared-memory staged SGD kernel.
 //
 // Persistent CTAs take work units (runs of consecutive scheduled slots, in
-// schedule order) from a global counter.  For each tile of the slot's block (see tiles.cpp):
+// schedule order) from a global counter, one unit ahead of the one they work
+// on, and walk the tiles of the unit's slots as one stream, fetching each next
+// tile's header and staged row ids while the current tile computes.  For each
+// tile of the slot's block (see tiles.cpp):
 //   1. stage   every distinct row of the tile, its entries and CSR lists are
 //              copied from L2 into shared memory (snapshot S) with 16-byte
 //              cp.async copies spread over the whole CTA, all in flight at once;
 //   2. errors  one lane group per entry: dot of the three staged rows,
 //              shuffle-reduced, err = value - dot;
 //   3. owners  one lane group per owner segment (a run of <= seg entries
-//              sharing a row of one mode) sums err * (other two rows) from S
+//              sharing a row of one mode; a tile's segments come longest
+//              first, so a warp's lane groups run loops of about equal
+//              length) sums err * (other two rows) from S
 //              in registers and adds coe*lr*(sum - count*reg*row) to the row
 //              (row: the snapshot; for a FAST row, its value at write time)
-//              in global memory with one vector atomic per 16 bytes (BF16
+//              in global memory with one vector red per 16 bytes (BF16
 //              rows without a master: the stochastically rounded difference
-//              to the snapshot, by bf16x2 atomic adds), so a row is written
-//              once per segment instead of once per entry.
+//              to the snapshot, by predicated bf16x2 reds), so a row is
+//              written once per segment instead of once per entry.
 // Inside a tile the update is the reference kernel's: all entries of one
 // thread_size wave read rows before their deltas land (sgd_Kernel.cu:358-392),
 // coe-weighted, L2-regularised per visit.  Tiles of one slot run in order on
