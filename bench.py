@@ -429,8 +429,8 @@ def judge_learned(w, dtype, mode, device, elearn, args):
     tr_h = _trajectory(ch, w, elearn, rates=(LEARN["lr"], LEARN["reg"]), train_every=5)
     tr_l = _trajectory(cl, w, elearn, rates=(LEARN["lr"], LEARN["reg"]), train_every=5)
     target = 1.01 * min(tr_h[-1][2], tr_l[-1][2])
-    _, t_h = _time_to(tr_h, target)
-    _, t_l = _time_to(tr_l, target)
+    e_h, t_h = _time_to(tr_h, target)
+    e_l, t_l = _time_to(tr_l, target)
     kept = t_l is not None and (t_h is None or t_l < t_h)
     rep = {"kept": bool(kept),
            "judge": "on the first %d cells: device time to 1.01 x the better final test RMSE of the two, learning "
@@ -439,6 +439,7 @@ def judge_learned(w, dtype, mode, device, elearn, args):
            "updates_per_epoch_learned": int(sl.summary.scheduled_updates),
            "updates_per_epoch_reference": int(sh.summary.scheduled_updates),
            "time_to_target_ms_learned": t_l, "time_to_target_ms_reference": t_h,
+           "epochs_to_target_learned": e_l, "epochs_to_target_reference": e_h,
            "final_test_rmse_learned": tr_l[-1][2], "final_test_rmse_reference": tr_h[-1][2],
            "blocks_learned": int(sl.summary.num_blocks), "groups_learned": int(sl.summary.num_groups),
            "build_seconds_learned": round(build_s, 2)}
@@ -546,12 +547,30 @@ def run_gpu(args):
         learned, model, kept = judge_learned(w, dtype, mode, local, elearn, args)
         ph.mark("learned_judge")
         if kept:
+            # the sample judged the trajectories; the whole workload decides
+            # the epoch times: the learned blocking stays only if its epochs to
+            # the target times its epoch time here is the shorter device time
+            ms_h_full = _epoch_ms(ctx, 2)
             sched_l = bg.Schedule(cfg, tx, learned=True, model=model)
             ctx_l = ctx_on(sched_l, dtype, mode)
             ctx_l.train_epochs(args.warmup)
             tune_l = ctx_l.autotune(2) if not args.no_tune else None
-            ctx.close()
-            ctx, sched, tune = ctx_l, sched_l, tune_l
+            ms_l_full = _epoch_ms(ctx_l, 2)
+            e_l, e_h = learned["epochs_to_target_learned"], learned["epochs_to_target_reference"]
+            proj_l = e_l * ms_l_full
+            proj_h = e_h * ms_h_full if e_h else None
+            kept = proj_h is None or proj_l < proj_h
+            learned.update({"kept": bool(kept), "kept_on_sample": True, "epoch_ms_full_learned": ms_l_full,
+                            "epoch_ms_full_reference": ms_h_full, "projected_time_to_target_ms_learned": proj_l,
+                            "projected_time_to_target_ms_reference": proj_h})
+            log("learned blocking on the whole workload: %.2f vs %.2f ms/epoch; projected time to target %.1f vs "
+                "%s ms; kept %d" % (ms_l_full, ms_h_full, proj_l, "%.1f" % proj_h if proj_h else "-", kept))
+            if kept:
+                ctx.close()
+                ctx, sched, tune = ctx_l, sched_l, tune_l
+            else:
+                ctx_l.close()
+                sched_l.close()
             ph.mark("learned_blocking_full")
     upd_per_step = sched.summary.scheduled_updates
     rm0 = ctx.eval(bg.TEST).rmse
